@@ -1,0 +1,240 @@
+/*
+ * parent_gb300 — C ABI of the GB300 (sm_103a) engine for PARENT's hot path:
+ * all-pairs 2D-histogram entropies / mutual information over the bond, angle
+ * and dihedral degrees of freedom (DOFs) of a BAT trajectory, and the MIST
+ * maximum spanning tree over the resulting MI matrix.
+ *
+ * The reference (markusfleck/PARENT) exposes this path as processes and files:
+ *   PARENT.x in.bat out.par b1D a1D d1D b2D a2D d2D   (src/PARENT/PARENT.cpp:190-244)
+ *   get_PAR_MIST.x in.par out.txt                     (src/process_output/get_PAR_MIST.cpp:74-77)
+ *   get_PAR_MIE.x in.par, get_PAR_info.x in.par       (src/process_output/get_PAR_MIE.cpp:91, get_PAR_info.cpp:46)
+ * and the io library src/util/io/io_binary.h:42-52. Each entry point below
+ * names the reference code it replaces. The CLIs in parent_gb300/cli/ are
+ * drop-ins for those programs and are built on this ABI.
+ *
+ * Conventions (mirroring the reference's int-return io library,
+ * io_binary.cpp:101,199,602,643): every function returns a pg_status; 0 is
+ * success. No C++ exception crosses this boundary. The caller owns every host
+ * buffer it passes; the library owns device memory it allocates. One context
+ * per host thread; calls on one context are serialised on its CUDA stream.
+ *
+ * DOF numbering: nBonds = nDih + 2, nAngles = nDih + 1 (PARENT.cpp:298-299).
+ * Global DOF index g: bonds [0, nB), angles [nB, nB+nA), dihedrals after.
+ */
+#ifndef PARENT_GB300_H
+#define PARENT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PG_API __attribute__((visibility("default")))
+#else
+#define PG_API
+#endif
+
+typedef enum pg_status {
+    PG_OK = 0,
+    PG_ERR_ARG = 1,     /* bad argument (reference: usage message + MPI_Abort) */
+    PG_ERR_IO = 2,      /* open/read/write failure (reference: fstream failbit) */
+    PG_ERR_FORMAT = 3,  /* corrupted header (io_binary.cpp:127-145, :477-519, :558-591) */
+    PG_ERR_DATA = 4,    /* value outside the reference's valid domain: negative bond
+                           (PARENT.cpp:522-525) or a bin index outside [0,B) */
+    PG_ERR_CUDA = 5,    /* CUDA runtime error */
+    PG_ERR_NOMEM = 6,   /* allocation failure (reference: "ERROR ALLOCATNG MEMORY") */
+    PG_ERR_TIMEOUT = 7, /* a bounded device-side wait ran out (status read back, context kept) */
+    PG_ERR_UNSUPPORTED = 8
+} pg_status;
+
+/* Which pair-count kernel computes the 2D histograms. */
+typedef enum pg_form {
+    PG_FORM_AUTO = 0,   /* autotuner picks per (bins, frames, DOFs) */
+    PG_FORM_HIST = 1,   /* shared-memory histogram kernel (TMA-staged bins, smem atomics) */
+    PG_FORM_ONEHOT = 2  /* tcgen05 one-hot GEMM kernel (FP8 0/1 operands, FP32 TMEM accumulate) */
+} pg_form;
+
+typedef struct pg_ctx pg_ctx;
+
+/* Trajectory columns, DOF-major: column k of a block starts at base + k*ld
+ * elements and holds n_frames values. double_prec=1 -> double, 0 -> float
+ * (FP32 values are promoted to double before any arithmetic, as
+ * read_BAT_frame does, io_binary.cpp:322-364). on_device=1 -> pointers are
+ * device pointers on the context's device. */
+typedef struct pg_bat_view {
+    int n_dihedrals;
+    int n_frames;
+    int double_prec;
+    int on_device;
+    int64_t ld; /* elements between consecutive DOF columns (>= n_frames) */
+    const void *bonds;
+    const void *angles;
+    const void *dihedrals;
+} pg_bat_view;
+
+/* Entropy results in the exact .par body layout (write_PAR_body,
+ * io_binary.cpp:606-631): same-type blocks bb/aa/dd store pair #(P-1-k) at
+ * element k, i.e. reverse lexicographic order (PARENT.cpp:1107-1112);
+ * ba/bd/ad are row-major with the bond (resp. angle) index slow.
+ * Host pointers owned by the caller; sizes nB, nA, nD, nB(nB-1)/2, nB*nA,
+ * nB*nD, nA(nA-1)/2, nA*nD, nD(nD-1)/2 doubles. */
+typedef struct pg_par_body {
+    double *s1_b, *s1_a, *s1_d;
+    double *bb, *ba, *bd, *aa, *ad, *dd;
+} pg_par_body;
+
+/* One MIST edge as get_PAR_MIST.cpp:667 prints it: In type, Out type
+ * (0=b,1=a,2=d), 1-based In/Out DOF indices within their type, MI, and the
+ * number of DOFs still outside the tree before this edge's Out DOF joined. */
+typedef struct pg_mist_edge {
+    int type_in, type_out;
+    int index_in, index_out;
+    double mi;
+    int left;
+    int pad_;
+} pg_mist_edge;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device` with its own stream.
+ * Replaces the MPI_Init_thread/rank set-up of PARENT.cpp:131-145. */
+PG_API int pg_create(pg_ctx **out, int device);
+PG_API void pg_destroy(pg_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+PG_API const char *pg_last_error(const pg_ctx *ctx);
+/* Message of the last failing call that had no context (pg_create, file I/O). */
+PG_API const char *pg_last_global_error(void);
+
+/* --------------------------------------------------------- entropy engine */
+
+/* The PARENT.x computation (PARENT.cpp:443-1493 minus the file I/O): per-DOF
+ * extrema and dihedral shift, 1D entropies, every pair's 2D entropy, written
+ * into `out` in .par body layout. bins = {b1D, a1D, d1D, b2D, a2D, d2D}
+ * (the CLI order of PARENT.cpp:211-234); every bin count >= 1, 2D bin counts
+ * <= PG_MAX_BINS_2D. The MI matrix stays resident on the device for pg_mist.
+ * `out` may be NULL (results kept on the device only). */
+#define PG_MAX_BINS_2D 218
+PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                      pg_par_body *out);
+
+/* MIST (get_PAR_MIST.cpp:272-766). If body != NULL the MI values are formed
+ * from it exactly as get_mutual (util.cpp:47-81) does; if body == NULL the MI
+ * matrix resident from the last pg_entropy on this context is used.
+ * edges: nB+nA+nD-1 entries; totals[10] in get_PAR_MIST.cpp:756-765 order. */
+PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mist_edge *edges,
+                   double totals[10]);
+
+/* Device milliseconds of the kernels of the last pg_entropy / pg_mist call,
+ * measured with CUDA events on the context's stream:
+ * ms[0] = preprocessing (extrema, modfit, binning, 1D), ms[1] = pair kernel,
+ * ms[2] = MIST kernel, ms[3] = host<->device copies, ms[4] = whole call. */
+PG_API int pg_last_timings(const pg_ctx *ctx, double ms[5]);
+/* Kernel launches issued by this context since creation. */
+PG_API int64_t pg_launch_count(const pg_ctx *ctx);
+/* Form used by the last pg_entropy (PG_FORM_HIST or PG_FORM_ONEHOT). */
+PG_API int pg_last_form(const pg_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for event timing by callers. */
+PG_API void *pg_stream(const pg_ctx *ctx);
+
+/* Debug/parity export: runs the same preprocessing and pair-histogram kernel
+ * as pg_entropy for n_pairs explicit pairs (g1[k] < g2[k], global DOF
+ * indices) and copies their 2D counts (row-major, B(g1) x B(g2), int64) to
+ * counts + k*stride. The reference never exposes counts; this replaces
+ * nothing and exists so counts can be compared bit-exactly. */
+PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                          int n_pairs, const int *g1, const int *g2, int64_t *counts,
+                          int64_t stride);
+
+/* Per-DOF preprocessing results of the last pg_entropy (host arrays of D):
+ * min, max (after padding/clamps, PARENT.cpp:526-533,551-559,624-634) and
+ * the dihedral shift modFit (PARENT.cpp:609; 0 for bonds/angles). */
+PG_API int pg_dof_stats(pg_ctx *ctx, double *mn, double *mx, double *shift);
+
+/* ------------------------------------------------------------ file formats */
+
+/* Opaque .bat contents: header (atoms, dihedral table, masses) and DOF-major
+ * FP64 or FP32 columns in pinned host memory. Replaces read_BAT_header +
+ * read_BAT_frame (io_binary.cpp:107-200, :281-368) and PARENT's frame-major
+ * to DOF-major scatter (PARENT.cpp:443-473). */
+typedef struct pg_bat pg_bat;
+PG_API int pg_bat_read(const char *path, pg_bat **out);
+PG_API void pg_bat_free(pg_bat *bat);
+PG_API int pg_bat_view_of(const pg_bat *bat, pg_bat_view *view);
+PG_API int pg_bat_n_dihedrals(const pg_bat *bat);
+PG_API int pg_bat_n_frames(const pg_bat *bat);
+
+/* Writes a .bat (version 3) from DOF-major host columns with a synthetic
+ * linear-chain header (write_BAT_header / write_BAT_frame,
+ * io_binary.cpp:43-102, :203-278). Used for synthetic trajectories. */
+PG_API int pg_bat_write_synthetic(const char *path, const pg_bat_view *traj);
+
+/* Writes a .par: header from `bat` (write_PAR_header, io_binary.cpp:371-442,
+ * version 4) and body (write_PAR_body, :606-631). Byte-compatible with the
+ * reference's read_PAR_header/read_PAR_body. */
+PG_API int pg_par_write(const char *path, const pg_bat *bat, const int bins[6],
+                        const pg_par_body *body);
+
+/* Opaque .par contents (read_PAR_header + read_PAR_body, io_binary.cpp:446-673). */
+typedef struct pg_par pg_par;
+PG_API int pg_par_read(const char *path, pg_par **out);
+PG_API void pg_par_free(pg_par *par);
+PG_API int pg_par_n_dihedrals(const pg_par *par);
+PG_API int pg_par_body_of(const pg_par *par, pg_par_body *body);
+PG_API int pg_par_bins(const pg_par *par, int bins[6]);
+
+/* Text outputs, byte-identical to the reference programs' stdout/file:
+ * get_PAR_MIE.cpp:109-199 (MIE), get_PAR_MIST.cpp:667-765 (MIST),
+ * get_PAR_info.cpp:64-79 (topology). path NULL -> stdout. */
+PG_API int pg_write_mie_text(const char *path, int n_dihedrals, const pg_par_body *body);
+PG_API int pg_write_mist_text(const char *path, int n_dihedrals, const pg_mist_edge *edges,
+                              const double totals[10]);
+PG_API int pg_write_info_text(const char *path, const pg_par *par);
+
+/* ------------------------------------------------------ synthetic workload */
+
+/* Seeded synthetic linear-chain trajectory (n_atoms atoms -> nDih = n_atoms-3)
+ * written DOF-major into caller buffers (host: pg_synth_host, device:
+ * pg_synth_device on ctx's device). Bonds ~ Normal(0.15, 0.005), angles ~
+ * von Mises(1.91, 40) clipped inside (0, pi), dihedrals ~ mixture of 1-3
+ * von Mises modes wrapped to [0, 2pi), correlated through n_latents AR(1)
+ * latents (phi = 0.95) mixed with Normal(0, 0.3) weights.
+ * frac_bimodal_dih / frac_bimodal_bond: fraction of dihedrals (bonds) whose
+ * mode follows a two-state Markov chain with switch probability p_switch. */
+typedef struct pg_synth_spec {
+    int n_atoms;
+    int n_frames;
+    int double_prec;
+    int n_latents;
+    uint64_t seed;
+    double frac_bimodal_dih;
+    double frac_bimodal_bond;
+    double p_switch;
+} pg_synth_spec;
+PG_API int pg_synth_host(const pg_synth_spec *spec, void *bonds, void *angles, void *dihedrals,
+                         int64_t ld, int n_threads);
+PG_API int pg_synth_device(pg_ctx *ctx, const pg_synth_spec *spec, void *bonds, void *angles,
+                           void *dihedrals, int64_t ld);
+
+/* Roofline probe (no reference counterpart): rate of warp-wide shared-memory
+ * reductions with every lane on its own bank, over all SMs of the context's
+ * device. It is the peak the histogram pair kernel is measured against. */
+PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s);
+
+/* ------------------------------------------------------ device memory */
+
+/* Device allocations owned by the caller through the library (so callers
+ * need no CUDA runtime of their own). */
+PG_API int pg_device_alloc(pg_ctx *ctx, size_t bytes, void **ptr);
+PG_API int pg_device_free(pg_ctx *ctx, void *ptr);
+PG_API int pg_memcpy(pg_ctx *ctx, void *dst, const void *src, size_t bytes, int kind /* 1 H2D, 2 D2H, 3 D2D */);
+PG_API int pg_host_alloc_pinned(size_t bytes, void **ptr);
+PG_API int pg_host_free_pinned(void *ptr);
+PG_API int pg_synchronize(pg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

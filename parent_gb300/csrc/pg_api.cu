@@ -1,0 +1,599 @@
+// C ABI implementation: context, device buffers, and the orchestration of the
+// preprocessing, pair and MIST kernels (host code; kernels live in the other
+// translation units).
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/parent_gb300.h"
+#include "pg_internal.h"
+
+namespace pg {
+
+size_t prep_smem_bytes(const SysGeom &g);
+size_t mist_scratch_bytes(int D);
+cudaError_t launch_mist_impl(int D, int nb, int na, const double *mi, void *scratch,
+                             double *edge_mi, int *edge_from, int *edge_to, cudaStream_t st);
+bool synth_spec_ok(const pg_synth_spec *sp);
+size_t synth_scratch_bytes(const pg_synth_spec *sp, size_t *lat_bytes, size_t *sw_bytes,
+                           std::vector<float> &lat, std::vector<int> &sw, std::vector<int> &sw_off);
+cudaError_t launch_synth_dev(const pg_synth_spec *sp, void *b, void *a, void *d, int64_t ld,
+                             const float *lat, const int *sw, const int *sw_off, cudaStream_t st);
+int autotune_form(const SysGeom &g);
+void set_global_error(const char *msg);
+double probe_smem_red_rate(int n_sm, cudaStream_t st, int *launches);
+
+ParLayout par_layout(int n_dih) {
+    const int64_t nb = n_dih + 2, na = n_dih + 1, nd = n_dih;
+    ParLayout L;
+    L.s1b = 0;
+    L.s1a = L.s1b + nb;
+    L.s1d = L.s1a + na;
+    L.bb = L.s1d + nd;
+    L.ba = L.bb + nb * (nb - 1) / 2;
+    L.bd = L.ba + nb * na;
+    L.aa = L.bd + nb * nd;
+    L.ad = L.aa + na * (na - 1) / 2;
+    L.dd = L.ad + na * nd;
+    L.total = L.dd + nd * (nd - 1) / 2;
+    return L;
+}
+
+// Tiles of T x T DOFs over the upper triangle of the DOF x DOF grid, in
+// super-blocks of 16 x 16 tiles so that CTAs resident at the same time share
+// their bin rows in L2.
+std::vector<PairTile> build_tiles(int D, int T) {
+    const int nblk = (D + T - 1) / T, S = 16, nsb = (nblk + S - 1) / S;
+    std::vector<PairTile> t;
+    t.reserve((size_t)nblk * (nblk + 1) / 2);
+    for (int sc = 0; sc < nsb; sc++)
+        for (int sr = 0; sr <= sc; sr++)
+            for (int cb = sc * S; cb < std::min(nblk, (sc + 1) * S); cb++)
+                for (int rb = sr * S; rb < std::min(nblk, (sr + 1) * S) && rb <= cb; rb++)
+                    t.push_back(PairTile{rb * T, cb * T, std::min(T, D - rb * T), std::min(T, D - cb * T)});
+    return t;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+namespace {
+
+thread_local std::string g_global_err;
+
+}  // namespace
+
+void pg::set_global_error(const char *msg) { g_global_err = msg; }
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t b = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) n = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct pg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string err;
+    DevBuf cols, bins, dofbuf, par, mi, nlogn, tiles, errw, scratch, counts, edges, mistscr;
+    int nlogn_max = -1;
+    std::vector<PairTile> tiles_host;
+    int tiles_D = -1, tiles_T = -1;
+    int64_t launches = 0;
+    double timings[5] = {0, 0, 0, 0, 0};
+    int last_form = 0;
+    bool resident = false;  // MI matrix of the last pg_entropy is valid
+    SysGeom geo{};
+};
+
+static int fail(pg_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf; else g_global_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PG_ERR_NOMEM : PG_ERR_CUDA, "%s: %s", \
+                        #call, cudaGetErrorString(e_));                                              \
+    } while (0)
+
+static DofArrays dof_arrays(pg_ctx *ctx, int D) {
+    DofArrays d;
+    double *base = (double *)ctx->dofbuf.p;
+    d.mn = base;
+    d.mx = base + D;
+    d.shift = base + 2 * (size_t)D;
+    d.s1 = base + 3 * (size_t)D;
+    d.acon = base + 4 * (size_t)D;
+    d.b2 = (int *)(base + 5 * (size_t)D);
+    return d;
+}
+
+static size_t elem_size(int prec) { return prec ? 8 : 4; }
+
+// Shared front half of pg_entropy / pg_pair_counts: validation, upload,
+// preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
+static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
+    if (!tv || !bins) return fail(ctx, PG_ERR_ARG, "null trajectory or bins");
+    if (tv->n_dihedrals < 0 || tv->n_frames < 1)
+        return fail(ctx, PG_ERR_ARG, "n_dihedrals (%d) < 0 or n_frames (%d) < 1", tv->n_dihedrals, tv->n_frames);
+    if (tv->double_prec != 0 && tv->double_prec != 1)
+        return fail(ctx, PG_ERR_ARG, "double_prec must be 0 or 1");
+    if (tv->ld < tv->n_frames) return fail(ctx, PG_ERR_ARG, "ld < n_frames");
+    if (!tv->bonds || !tv->angles || (tv->n_dihedrals > 0 && !tv->dihedrals))
+        return fail(ctx, PG_ERR_ARG, "null column pointer");
+    for (int k = 0; k < 6; k++) {
+        if (bins[k] < 1) return fail(ctx, PG_ERR_ARG, "bin count %d (index %d) < 1", bins[k], k);
+        if (k < 3 && bins[k] > 16384) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin count %d > 16384", bins[k]);
+        if (k >= 3 && bins[k] > PG_MAX_BINS_2D)
+            return fail(ctx, PG_ERR_UNSUPPORTED, "2D bin count %d > %d", bins[k], PG_MAX_BINS_2D);
+    }
+    CK(cudaSetDevice(ctx->device));
+    SysGeom &g = ctx->geo;
+    g.n_dih = tv->n_dihedrals;
+    g.nb = g.n_dih + 2;
+    g.na = g.n_dih + 1;
+    g.nd = g.n_dih;
+    g.D = g.nb + g.na + g.nd;
+    g.F = tv->n_frames;
+    g.ldb = ((int64_t)g.F + 4095) / 4096 * 4096;
+    for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
+    ctx->resident = false;
+    const int D = g.D;
+    cudaStream_t st = ctx->stream;
+
+    CK(cudaEventRecord(ctx->ev[0], st));
+    // columns
+    const void *cols[3];
+    int64_t ld = tv->ld;
+    if (tv->on_device) {
+        cols[0] = tv->bonds;
+        cols[1] = tv->angles;
+        cols[2] = tv->dihedrals ? tv->dihedrals : tv->angles;
+    } else {
+        const size_t es = elem_size(tv->double_prec);
+        ld = tv->n_frames;
+        const size_t blk[3] = {(size_t)g.nb * ld * es, (size_t)g.na * ld * es, (size_t)g.nd * ld * es};
+        CK(ctx->cols.ensure(blk[0] + blk[1] + blk[2] + 256));
+        char *dst = (char *)ctx->cols.p;
+        const void *src[3] = {tv->bonds, tv->angles, tv->dihedrals};
+        const int cnt[3] = {g.nb, g.na, g.nd};
+        for (int t = 0; t < 3; t++) {
+            cols[t] = dst;
+            if (cnt[t] > 0) {
+                if (tv->ld == tv->n_frames) {
+                    CK(cudaMemcpyAsync(dst, src[t], blk[t], cudaMemcpyHostToDevice, st));
+                } else {
+                    CK(cudaMemcpy2DAsync(dst, ld * es, src[t], tv->ld * es, ld * es, cnt[t],
+                                         cudaMemcpyHostToDevice, st));
+                }
+            }
+            dst += blk[t];
+        }
+        if (g.nd == 0) cols[2] = cols[1];
+    }
+    CK(cudaEventRecord(ctx->ev[1], st));
+
+    CK(ctx->bins.ensure((size_t)D * g.ldb));
+    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + sizeof(int)) + 64));
+    CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
+    if (ctx->nlogn_max < g.F) {
+        CK(ctx->nlogn.ensure(((size_t)g.F + 1) * sizeof(double)));
+        CK(launch_nlogn_table((double *)ctx->nlogn.p, g.F, st));
+        ctx->launches++;
+        ctx->nlogn_max = g.F;
+    }
+    if (prep_smem_bytes(g) > 200 * 1024) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin counts too large");
+    CK(launch_prep(g, cols, ld, tv->double_prec, dof_arrays(ctx, D), (uint8_t *)ctx->bins.p,
+                   (int *)ctx->errw.p, st));
+    ctx->launches++;
+    CK(cudaEventRecord(ctx->ev[2], st));
+    return PG_OK;
+}
+
+static int check_err_words(pg_ctx *ctx) {
+    int h[ERR_WORDS];
+    CK(cudaMemcpyAsync(h, ctx->errw.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (h[ERR_NEG_BOND]) return fail(ctx, PG_ERR_DATA, "ERROR: %d bond(s) smaller than 0.0", h[ERR_NEG_BOND]);
+    if (h[ERR_MODFIT_RANGE])
+        return fail(ctx, PG_ERR_DATA, "%d dihedral value(s) outside [0, 2pi+5e-9) (shift histogram)", h[ERR_MODFIT_RANGE]);
+    if (h[ERR_BIN_RANGE]) return fail(ctx, PG_ERR_DATA, "%d bin index(es) outside [0, B)", h[ERR_BIN_RANGE]);
+    if (h[ERR_TIMEOUT]) return fail(ctx, PG_ERR_TIMEOUT, "a device-side wait timed out (%d CTA(s))", h[ERR_TIMEOUT]);
+    return PG_OK;
+}
+
+static int bmax_of(const SysGeom &g) {
+    return std::max(g.bins[3], std::max(g.bins[4], g.bins[5]));
+}
+
+extern "C" {
+
+PG_API const char *pg_last_global_error(void) { return g_global_err.c_str(); }
+
+PG_API int pg_create(pg_ctx **out, int device) {
+    if (!out) return fail(nullptr, PG_ERR_ARG, "null out");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, PG_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    if (device < 0 || device >= n) return fail(nullptr, PG_ERR_ARG, "device %d out of range", device);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, PG_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    pg_ctx *c = new pg_ctx;
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaEventCreate(&c->ev[k]);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(nullptr, PG_ERR_CUDA, "stream/event creation: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return PG_OK;
+}
+
+PG_API void pg_destroy(pg_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn,
+                      &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr})
+        b->release();
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+PG_API const char *pg_last_error(const pg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_global_err.c_str(); }
+
+PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                      pg_par_body *out) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (form < PG_FORM_AUTO || form > PG_FORM_ONEHOT) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    int rc = run_prep(ctx, traj, bins);
+    if (rc) return rc;
+    const SysGeom &g = ctx->geo;
+    cudaStream_t st = ctx->stream;
+    const ParLayout L = par_layout(g.n_dih);
+    CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
+    CK(ctx->mi.ensure((size_t)g.D * g.D * sizeof(double)));
+    DofArrays dof = dof_arrays(ctx, g.D);
+    // 1D entropies into the .par body (bonds, angles, dihedrals are contiguous
+    // in both the DOF arrays and the body)
+    CK(cudaMemcpyAsync((double *)ctx->par.p + L.s1b, dof.s1, (size_t)g.D * sizeof(double),
+                       cudaMemcpyDeviceToDevice, st));
+
+    int chosen = form == PG_FORM_AUTO ? autotune_form(g) : form;
+    if (chosen == PG_FORM_ONEHOT && !pairs_onehot_supported(g)) {
+        if (form == PG_FORM_ONEHOT)
+            return fail(ctx, PG_ERR_UNSUPPORTED, "one-hot tensor-core form unsupported for this geometry");
+        chosen = PG_FORM_HIST;
+    }
+    PairOut po;
+    po.par = (double *)ctx->par.p;
+    po.mi = (double *)ctx->mi.p;
+    po.L = L;
+    po.counts = nullptr;
+    po.counts_bmax = 0;
+    if (chosen == PG_FORM_HIST) {
+        int T = 0, fc = 0;
+        if (!pairs_hist_config(bmax_of(g), &T, &fc)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+        if (ctx->tiles_D != g.D || ctx->tiles_T != T) {
+            ctx->tiles_host = build_tiles(g.D, T);
+            CK(ctx->tiles.ensure(ctx->tiles_host.size() * sizeof(PairTile)));
+            CK(cudaMemcpyAsync(ctx->tiles.p, ctx->tiles_host.data(), ctx->tiles_host.size() * sizeof(PairTile),
+                               cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));  // host vector may be rebuilt later
+            ctx->tiles_D = g.D;
+            ctx->tiles_T = T;
+        }
+        CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const double *)ctx->nlogn.p,
+                             (const PairTile *)ctx->tiles.p, (int64_t)ctx->tiles_host.size(), T, po,
+                             (int *)ctx->errw.p, st));
+        ctx->launches++;
+    } else {
+        const size_t sb = pairs_onehot_scratch_bytes(g);
+        CK(ctx->scratch.ensure(sb));
+        int nl = 0;
+        CK(launch_pairs_onehot(g, (const uint8_t *)ctx->bins.p, dof, (const double *)ctx->nlogn.p, po,
+                               (int *)ctx->errw.p, st, ctx->scratch.p, sb, &nl));
+        ctx->launches += nl;
+    }
+    ctx->last_form = chosen;
+    CK(cudaEventRecord(ctx->ev[3], st));
+    if (out) {
+        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
+        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
+        for (int k = 0; k < 9; k++) {
+            const int64_t n = off[k + 1] - off[k];
+            if (n <= 0) continue;
+            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
+            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+        }
+    }
+    CK(cudaEventRecord(ctx->ev[4], st));
+    rc = check_err_words(ctx);
+    float ms[4];
+    cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&ms[2], ctx->ev[2], ctx->ev[3]);
+    cudaEventElapsedTime(&ms[3], ctx->ev[3], ctx->ev[4]);
+    ctx->timings[0] = ms[1];
+    ctx->timings[1] = ms[2];
+    ctx->timings[3] = ms[0] + ms[3];
+    ctx->timings[4] = ms[0] + ms[1] + ms[2] + ms[3];
+    if (rc) return rc;
+    ctx->resident = true;
+    return PG_OK;
+}
+
+PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                          int n_pairs, const int *g1, const int *g2, int64_t *counts, int64_t stride) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (n_pairs < 0 || (n_pairs > 0 && (!g1 || !g2 || !counts))) return fail(ctx, PG_ERR_ARG, "bad pair list");
+    if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "count export uses the histogram form");
+    int rc = run_prep(ctx, traj, bins);
+    if (rc) return rc;
+    const SysGeom &g = ctx->geo;
+    std::vector<PairTile> t((size_t)n_pairs);
+    for (int k = 0; k < n_pairs; k++) {
+        if (g1[k] < 0 || g2[k] >= g.D || g1[k] >= g2[k])
+            return fail(ctx, PG_ERR_ARG, "pair %d: need 0 <= g1 < g2 < D", k);
+        t[k] = PairTile{g1[k], g2[k], 1, 1};
+        const int b1 = g.bins[3 + dof_type(g1[k], g.nb, g.na)], b2 = g.bins[3 + dof_type(g2[k], g.nb, g.na)];
+        if (stride < (int64_t)b1 * b2) return fail(ctx, PG_ERR_ARG, "stride < B1*B2");
+    }
+    if (n_pairs == 0) return PG_OK;
+    int T = 0, fc = 0;
+    const int bm = bmax_of(g);
+    if (!pairs_hist_config(bm, &T, &fc)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+    const int pps = T * T;
+    cudaStream_t st = ctx->stream;
+    DevBuf tiles;  // private: keep the cached full tile list intact
+    CK(tiles.ensure(t.size() * sizeof(PairTile)));
+    CK(ctx->counts.ensure((size_t)n_pairs * pps * bm * bm * sizeof(int64_t)));
+    CK(cudaMemcpyAsync(tiles.p, t.data(), t.size() * sizeof(PairTile), cudaMemcpyHostToDevice, st));
+    PairOut po;
+    po.par = nullptr;
+    po.mi = nullptr;
+    po.L = par_layout(g.n_dih);
+    po.counts = (int64_t *)ctx->counts.p;
+    po.counts_bmax = bm;
+    cudaError_t e = launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof_arrays(ctx, g.D),
+                                      (const double *)ctx->nlogn.p, (const PairTile *)tiles.p, n_pairs, T,
+                                      po, (int *)ctx->errw.p, st);
+    ctx->launches++;
+    if (e == cudaSuccess) {
+        for (int k = 0; k < n_pairs && e == cudaSuccess; k++) {
+            const int b1 = g.bins[3 + dof_type(g1[k], g.nb, g.na)], b2 = g.bins[3 + dof_type(g2[k], g.nb, g.na)];
+            e = cudaMemcpyAsync(counts + (int64_t)k * stride, (int64_t *)ctx->counts.p + (int64_t)k * pps * bm * bm,
+                                (size_t)b1 * b2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+        }
+    }
+    cudaStreamSynchronize(st);
+    tiles.release();
+    if (e != cudaSuccess) return fail(ctx, PG_ERR_CUDA, "pair count export: %s", cudaGetErrorString(e));
+    return check_err_words(ctx);
+}
+
+PG_API int pg_dof_stats(pg_ctx *ctx, double *mn, double *mx, double *shift) {
+    if (!ctx || !mn || !mx || !shift) return fail(ctx, PG_ERR_ARG, "null argument");
+    if (!ctx->dofbuf.p || ctx->geo.D == 0) return fail(ctx, PG_ERR_ARG, "no preprocessing results");
+    DofArrays d = dof_arrays(ctx, ctx->geo.D);
+    const size_t b = (size_t)ctx->geo.D * sizeof(double);
+    CK(cudaMemcpyAsync(mn, d.mn, b, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(mx, d.mx, b, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(shift, d.shift, b, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mist_edge *edges,
+                   double totals[10]) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (!edges || !totals) return fail(ctx, PG_ERR_ARG, "null edges/totals");
+    if (n_dihedrals < 0) return fail(ctx, PG_ERR_ARG, "n_dihedrals < 0");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int nb = n_dihedrals + 2, na = n_dihedrals + 1, nd = n_dihedrals, D = nb + na + nd;
+    const ParLayout L = par_layout(n_dihedrals);
+    std::vector<double> s1((size_t)D);
+    CK(cudaEventRecord(ctx->ev[0], st));
+    if (body) {
+        const double *src[9] = {body->s1_b, body->s1_a, body->s1_d, body->bb, body->ba, body->bd, body->aa, body->ad, body->dd};
+        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
+        CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
+        CK(ctx->mi.ensure((size_t)D * D * sizeof(double)));
+        for (int k = 0; k < 9; k++) {
+            const int64_t n = off[k + 1] - off[k];
+            if (n <= 0) continue;
+            if (!src[k]) return fail(ctx, PG_ERR_ARG, "null body block %d", k);
+            CK(cudaMemcpyAsync((double *)ctx->par.p + off[k], src[k], (size_t)n * sizeof(double),
+                               cudaMemcpyHostToDevice, st));
+        }
+        memcpy(s1.data(), body->s1_b, nb * sizeof(double));
+        memcpy(s1.data() + nb, body->s1_a, na * sizeof(double));
+        if (nd) memcpy(s1.data() + nb + na, body->s1_d, nd * sizeof(double));
+        CK(launch_mi_from_par(n_dihedrals, (const double *)ctx->par.p, L, (double *)ctx->mi.p, st));
+        ctx->launches++;
+        ctx->resident = false;
+    } else {
+        if (!ctx->resident || ctx->geo.n_dih != n_dihedrals)
+            return fail(ctx, PG_ERR_ARG, "no resident MI matrix for %d dihedrals", n_dihedrals);
+        CK(cudaMemcpyAsync(s1.data(), dof_arrays(ctx, D).s1, (size_t)D * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+    }
+    CK(ctx->edges.ensure((size_t)D * (sizeof(double) + 2 * sizeof(int)) + 256));
+    CK(ctx->mistscr.ensure(mist_scratch_bytes(D)));
+    double *emi = (double *)ctx->edges.p;
+    int *efrom = (int *)(emi + D), *eto = efrom + D;
+    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(launch_mist_impl(D, nb, na, (const double *)ctx->mi.p, ctx->mistscr.p, emi, efrom, eto, st));
+    ctx->launches++;
+    CK(cudaEventRecord(ctx->ev[2], st));
+    std::vector<double> hmi((size_t)D);
+    std::vector<int> hf((size_t)D), ht((size_t)D);
+    if (D > 1) {
+        CK(cudaMemcpyAsync(hmi.data(), emi, (size_t)(D - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hf.data(), efrom, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(ht.data(), eto, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaEventRecord(ctx->ev[3], st));
+    CK(cudaStreamSynchronize(st));
+    float ms[3];
+    cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&ms[2], ctx->ev[2], ctx->ev[3]);
+    ctx->timings[2] = ms[1];
+
+    // totals in get_PAR_MIST.cpp:279-287 and :663-765 order
+    double tB = 0, tA = 0, tD = 0, tm = 0, tp[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nb; k++) tB += s1[k];
+    for (int k = 0; k < na; k++) tA += s1[nb + k];
+    for (int k = 0; k < nd; k++) tD += s1[nb + na + k];
+    for (int s = 0; s < D - 1; s++) {
+        if (ht[s] < 0 || hf[s] < 0) return fail(ctx, PG_ERR_DATA, "MIST step %d found no candidate", s);
+        const int t1 = dof_type(hf[s], nb, na), t2 = dof_type(ht[s], nb, na);
+        const int off1 = t1 == TB ? 0 : (t1 == TA ? nb : nb + na);
+        const int off2 = t2 == TB ? 0 : (t2 == TA ? nb : nb + na);
+        edges[s].type_in = t1;
+        edges[s].type_out = t2;
+        edges[s].index_in = hf[s] - off1 + 1;
+        edges[s].index_out = ht[s] - off2 + 1;
+        edges[s].mi = hmi[s];
+        edges[s].left = D - 1 - s;
+        edges[s].pad_ = 0;
+        tm += hmi[s];
+        const int lo = std::min(t1, t2), hi = std::max(t1, t2);
+        tp[lo == 0 ? hi : (lo == 1 ? 2 + hi : 5)] += hmi[s];
+    }
+    totals[0] = tB;
+    totals[1] = tA;
+    totals[2] = tD;
+    for (int q = 0; q < 6; q++) totals[3 + q] = tp[q];
+    totals[9] = tB + tA + tD - tm;
+    return PG_OK;
+}
+
+PG_API int pg_last_timings(const pg_ctx *ctx, double ms[5]) {
+    if (!ctx || !ms) return PG_ERR_ARG;
+    for (int k = 0; k < 5; k++) ms[k] = ctx->timings[k];
+    return PG_OK;
+}
+PG_API int64_t pg_launch_count(const pg_ctx *ctx) { return ctx ? ctx->launches : -1; }
+PG_API int pg_last_form(const pg_ctx *ctx) { return ctx ? ctx->last_form : 0; }
+PG_API void *pg_stream(const pg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+PG_API int pg_synth_device(pg_ctx *ctx, const pg_synth_spec *spec, void *bonds, void *angles,
+                           void *dihedrals, int64_t ld) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    if (!synth_spec_ok(spec) || !bonds || !angles || (spec->n_atoms > 3 && !dihedrals) || ld < spec->n_frames)
+        return fail(ctx, PG_ERR_ARG, "bad synthetic spec or buffers");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float> lat;
+    std::vector<int> sw, sw_off;
+    size_t lb = 0, sb = 0;
+    const size_t total = synth_scratch_bytes(spec, &lb, &sb, lat, sw, sw_off);
+    DevBuf tmp;
+    CK(tmp.ensure(total));
+    char *base = (char *)tmp.p;
+    cudaStream_t st = ctx->stream;
+    if (!lat.empty()) CK(cudaMemcpyAsync(base, lat.data(), lat.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    int *dsw = (int *)(base + lb);
+    if (!sw.empty()) CK(cudaMemcpyAsync(dsw, sw.data(), sw.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    int *doff = dsw + sw.size();
+    CK(cudaMemcpyAsync(doff, sw_off.data(), sw_off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(launch_synth_dev(spec, bonds, angles, dihedrals ? dihedrals : angles, ld, (const float *)base, dsw, doff, st));
+    ctx->launches++;
+    CK(cudaStreamSynchronize(st));
+    tmp.release();
+    return PG_OK;
+}
+
+PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s) {
+    if (!ctx || !reductions_per_s) return fail(ctx, PG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    int n_sm = 0;
+    CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+    int nl = 0;
+    const double r = probe_smem_red_rate(n_sm, ctx->stream, &nl);
+    ctx->launches += nl;
+    if (r <= 0) return fail(ctx, PG_ERR_CUDA, "shared-memory reduction probe failed");
+    *reductions_per_s = r;
+    return PG_OK;
+}
+
+PG_API int pg_device_alloc(pg_ctx *ctx, size_t bytes, void **ptr) {
+    if (!ctx || !ptr) return fail(ctx, PG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMalloc(ptr, bytes));
+    return PG_OK;
+}
+PG_API int pg_device_free(pg_ctx *ctx, void *ptr) {
+    if (!ctx) return PG_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaFree(ptr));
+    return PG_OK;
+}
+PG_API int pg_memcpy(pg_ctx *ctx, void *dst, const void *src, size_t bytes, int kind) {
+    if (!ctx || kind < 1 || kind > 3) return fail(ctx, PG_ERR_ARG, "bad memcpy arguments");
+    const cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice : (kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+    CK(cudaMemcpyAsync(dst, src, bytes, k, ctx->stream));
+    return PG_OK;
+}
+PG_API int pg_host_alloc_pinned(size_t bytes, void **ptr) {
+    if (!ptr) return PG_ERR_ARG;
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) return fail(nullptr, PG_ERR_NOMEM, "cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return PG_OK;
+}
+PG_API int pg_host_free_pinned(void *ptr) {
+    cudaError_t e = cudaFreeHost(ptr);
+    return e == cudaSuccess ? PG_OK : fail(nullptr, PG_ERR_CUDA, "cudaFreeHost: %s", cudaGetErrorString(e));
+}
+PG_API int pg_synchronize(pg_ctx *ctx) {
+    if (!ctx) return PG_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// Internal declarations shared by the parent_gb300 CUDA translation units and
+// the host orchestration (pg_api.cu). Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pg {
+
+// DOF type codes (reference util.h:33-35).
+enum { TB = 0, TA = 1, TD = 2 };
+
+// Device-side error words, zeroed before each run and read back after it.
+enum {
+    ERR_BIN_RANGE = 0,    // a bin index fell outside [0, B) (reference: UB)
+    ERR_NEG_BOND = 1,     // a bond value < 0 (reference aborts, PARENT.cpp:522-525)
+    ERR_MODFIT_RANGE = 2, // a dihedral outside the modfit histogram (PARENT.cpp:571, UB)
+    ERR_TIMEOUT = 3,      // a bounded mbarrier / flag wait ran out
+    ERR_WORDS = 4
+};
+
+// Geometry of one system (one trajectory).
+struct SysGeom {
+    int n_dih, nb, na, nd, D;  // D = nb + na + nd
+    int F;                     // frames
+    int64_t ldb;               // bytes between DOF rows of the uint8 bin matrix
+    int bins[6];               // b1D a1D d1D b2D a2D d2D
+};
+
+__host__ __device__ inline int dof_type(int g, int nb, int na) {
+    return g < nb ? TB : (g < nb + na ? TA : TD);
+}
+
+// Per-DOF arrays produced by the preprocessing kernel (structure of arrays,
+// each D long, all in one device allocation).
+struct DofArrays {
+    double *mn, *mx, *shift; // extrema after padding/clamps; dihedral modFit
+    double *s1;              // 1D entropy (PARENT.cpp:650-757)
+    double *acon;            // ln(binsize_2D) + (1/N) sum_k m(k) ln J(k), the
+                             // per-DOF constant of the 2D entropy decomposition
+    int *b2;                 // 2D bin count of the DOF's type
+};
+
+// Offsets of the nine .par body blocks inside one contiguous double buffer.
+struct ParLayout {
+    int64_t s1b, s1a, s1d, bb, ba, bd, aa, ad, dd, total;
+};
+ParLayout par_layout(int n_dih);
+
+// Where the pair (g1 < g2) lands in the .par body (PARENT.cpp:896-898,
+// 1107-1112; reader util.cpp:55,67,76).
+__host__ __device__ inline int64_t par_pair_index(const ParLayout &L, int nb, int na, int nd,
+                                                  int g1, int g2) {
+    const int t1 = dof_type(g1, nb, na), t2 = dof_type(g2, nb, na);
+    const int i1 = g1 - (t1 == TB ? 0 : (t1 == TA ? nb : nb + na));
+    const int i2 = g2 - (t2 == TB ? 0 : (t2 == TA ? nb : nb + na));
+    if (t1 == t2) {
+        const int n = t1 == TB ? nb : (t1 == TA ? na : nd);
+        const int64_t base = t1 == TB ? L.bb : (t1 == TA ? L.aa : L.dd);
+        return base + (int64_t)(n - i1) * (n - i1 - 1) / 2 + i1 - i2;
+    }
+    if (t1 == TB && t2 == TA) return L.ba + (int64_t)i1 * na + i2;
+    if (t1 == TB) return L.bd + (int64_t)i1 * nd + i2;
+    return L.ad + (int64_t)i1 * nd + i2;
+}
+
+// A pair tile: row DOFs [row0, row0+nrow), column DOFs [col0, col0+ncol);
+// pair (r, c) is valid when r < c.
+struct PairTile {
+    int row0, col0;
+    int nrow, ncol;
+};
+
+// ---------------------------------------------------------------- launchers
+// All launchers enqueue on `st` and return cudaGetLastError().
+
+// nlogn[n] = n ln n for n in [0, nmax] (FP64).
+cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st);
+
+// Extrema + modfit + binning + 1D entropies + 2D decomposition constants.
+// cols[t] = device base of the type-t block (columns ld elements apart).
+cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
+                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st);
+
+// Shared-memory histogram pair kernel with fused entropy/MI epilogue.
+// If counts != nullptr the raw 2D histograms of each tile's first pair slots
+// are dumped (debug export) instead of the .par/MI outputs.
+struct PairOut {
+    double *par;        // .par body on device
+    double *mi;         // D x D dense MI (may be nullptr)
+    ParLayout L;
+    int64_t *counts;    // debug dump, per tile: 16 pair slots x Bmax^2 (nullptr normally)
+    int counts_bmax;
+};
+cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                              const double *nlogn, const PairTile *tiles, int64_t n_tiles,
+                              int tile_dim, PairOut out, int *err, cudaStream_t st);
+// smem bytes the histogram kernel needs for a given max 2D bin count, or 0 if
+// it cannot run; sets *tile_dim (4, 2 or 1 DOFs per tile side).
+int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames);
+
+// tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
+cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                                const double *nlogn, PairOut out, int *err, cudaStream_t st,
+                                void *scratch, size_t scratch_bytes, int *launches);
+size_t pairs_onehot_scratch_bytes(const SysGeom &g);
+bool pairs_onehot_supported(const SysGeom &g);
+
+// MI matrix from a .par body already on the device (get_mutual semantics).
+cudaError_t launch_mi_from_par(int n_dih, const double *par, ParLayout L, double *mi,
+                               cudaStream_t st);
+
+}  // namespace pg

@@ -1,0 +1,537 @@
+// File formats of the reference suite, host side:
+//   .bat  read_BAT_header / read_BAT_frame   (io_binary.cpp:107-200, :281-368)
+//         write_BAT_header / write_BAT_frame (io_binary.cpp:43-102, :203-278)
+//   .par  write_PAR_header / write_PAR_body  (io_binary.cpp:371-442, :606-631)
+//         read_PAR_header / read_PAR_body    (io_binary.cpp:446-673)
+//   text  get_PAR_MIE (get_PAR_MIE.cpp:109-199), get_PAR_MIST (get_PAR_MIST.cpp:667-765),
+//         get_PAR_info (get_PAR_info.cpp:64-79)
+// The .bat body is frame-major; it is transposed here into DOF-major columns
+// kept in the file's own precision (pinned host memory), which is the layout
+// the device kernels read.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/parent_gb300.h"
+
+namespace {
+
+}  // namespace
+
+namespace pg {
+void set_global_error(const char *msg);
+}
+
+namespace {
+
+// Records the message for pg_last_global_error and prints it to stderr, as
+// the reference's io library does.
+int ioerr(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    pg::set_global_error(buf);
+    fprintf(stderr, "%s\n", buf);
+    return code;
+}
+
+struct Header {
+    int version = 3, double_prec = 1, n_dih = 0, n_frames = 0;
+    std::vector<std::string> residues, atoms, molecules;
+    std::vector<int> resnums;
+    std::vector<int> dih;  // 6 per dihedral
+    std::vector<float> masses;
+};
+
+bool rd(FILE *f, void *p, size_t n) { return fread(p, 1, n, f) == n; }
+bool wr(FILE *f, const void *p, size_t n) { return fwrite(p, 1, n, f) == n; }
+
+std::string cstr(const char *p, size_t n) {
+    size_t k = 0;
+    while (k < n && p[k]) k++;
+    return std::string(p, k);
+}
+
+// atom block as write_BAT_header / write_PAR_header emit it: "%.7s" into 8
+// zeroed bytes, int, "%.7s" into 8 zeroed bytes, "%.30s" into 31 zeroed bytes
+bool write_atoms(FILE *f, const Header &h) {
+    for (int i = 0; i < h.n_dih + 3; i++) {
+        char b8[8], b31[31];
+        memset(b8, 0, 8);
+        strncpy(b8, h.residues[i].c_str(), 7);
+        if (!wr(f, b8, 8) || !wr(f, &h.resnums[i], 4)) return false;
+        memset(b8, 0, 8);
+        strncpy(b8, h.atoms[i].c_str(), 7);
+        if (!wr(f, b8, 8)) return false;
+        memset(b31, 0, 31);
+        strncpy(b31, h.molecules[i].c_str(), 30);
+        if (!wr(f, b31, 31)) return false;
+    }
+    return true;
+}
+
+bool read_atoms(FILE *f, Header &h) {
+    const int n = h.n_dih + 3;
+    h.residues.resize(n);
+    h.atoms.resize(n);
+    h.molecules.resize(n);
+    h.resnums.resize(n);
+    for (int i = 0; i < n; i++) {
+        char b8[8], b31[31];
+        if (!rd(f, b8, 8)) return false;
+        h.residues[i] = cstr(b8, 8);
+        if (!rd(f, &h.resnums[i], 4)) return false;
+        if (!rd(f, b8, 8)) return false;
+        h.atoms[i] = cstr(b8, 8);
+        if (!rd(f, b31, 31)) return false;
+        h.molecules[i] = cstr(b31, 31);
+    }
+    return true;
+}
+
+void synthetic_header(Header &h) {
+    const int n = h.n_dih + 3;
+    h.residues.assign(n, "SYN");
+    h.atoms.resize(n);
+    h.molecules.assign(n, "synthetic_chain");
+    h.resnums.resize(n);
+    h.masses.assign(n, 12.011f);
+    for (int i = 0; i < n; i++) {
+        h.atoms[i] = "C" + std::to_string(i + 1);
+        h.resnums[i] = i / 10 + 1;
+    }
+    h.dih.resize((size_t)6 * h.n_dih);
+    for (int i = 0; i < h.n_dih; i++) {  // linear chain: dihedral i = atoms i+1..i+4 (1-based)
+        for (int k = 0; k < 4; k++) h.dih[6 * i + k] = i + 1 + k;
+        h.dih[6 * i + 4] = 0;
+        h.dih[6 * i + 5] = -1;
+    }
+}
+
+}  // namespace
+
+struct pg_bat {
+    Header h;
+    void *cols = nullptr;  // pinned, DOF-major, bonds | angles | dihedrals
+    bool pinned = false;
+    size_t bytes = 0;
+};
+
+struct pg_par {
+    Header h;
+    int bins[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<double> body;
+    int64_t off[10];
+};
+
+static void layout(int nd_, int64_t off[10]) {
+    const int64_t nb = nd_ + 2, na = nd_ + 1, nd = nd_;
+    const int64_t sz[9] = {nb, na, nd, nb * (nb - 1) / 2, nb * na, nb * nd, na * (na - 1) / 2, na * nd, nd * (nd - 1) / 2};
+    off[0] = 0;
+    for (int k = 0; k < 9; k++) off[k + 1] = off[k] + sz[k];
+}
+
+extern "C" {
+
+PG_API int pg_bat_read(const char *path, pg_bat **out) {
+    if (!path || !out) return ioerr(PG_ERR_ARG, "pg_bat_read: null argument");
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: Could not open file %s !", path);
+    pg_bat *b = new pg_bat;
+    Header &h = b->h;
+    int rc = PG_OK;
+    do {
+        if (!rd(f, &h.version, 4) || !rd(f, &h.double_prec, 4) || !rd(f, &h.n_dih, 4) || !rd(f, &h.n_frames, 4)) {
+            rc = ioerr(PG_ERR_IO, "ERROR: could not read the header of %s", path);
+            break;
+        }
+        // the checks of read_BAT_header, io_binary.cpp:127-145
+        if (h.version < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version); break; }
+        if (h.double_prec != 0 && h.double_prec != 1) {
+            rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!", h.double_prec);
+            break;
+        }
+        if (h.n_dih > 19997) fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n", h.n_dih + 3);
+        if (h.n_dih < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih); break; }
+        if (h.n_frames < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames); break; }
+        if (h.version >= 3) {
+            if (!read_atoms(f, h)) { rc = ioerr(PG_ERR_IO, "ERROR: truncated atom block in %s", path); break; }
+        } else {
+            synthetic_header(h);  // pre-3 files carry no atom names
+        }
+        h.dih.resize((size_t)6 * h.n_dih);
+        h.masses.resize((size_t)h.n_dih + 3);
+        if ((h.n_dih && !rd(f, h.dih.data(), h.dih.size() * 4)) || !rd(f, h.masses.data(), h.masses.size() * 4)) {
+            rc = ioerr(PG_ERR_IO, "ERROR: truncated dihedral/mass block in %s", path);
+            break;
+        }
+        const int nb = h.n_dih + 2, na = h.n_dih + 1, nd = h.n_dih;
+        const size_t F = (size_t)h.n_frames, es = h.double_prec ? 8 : 4;
+        const size_t D = (size_t)nb + na + nd;
+        b->bytes = D * F * es;
+        if (cudaHostAlloc(&b->cols, b->bytes, cudaHostAllocDefault) == cudaSuccess) {
+            b->pinned = true;
+        } else {
+            cudaGetLastError();
+            b->cols = malloc(b->bytes);
+            if (!b->cols) { rc = ioerr(PG_ERR_NOMEM, "ERROR ALLOCATNG MEMORY! (%zu bytes)", b->bytes); break; }
+        }
+        // frames: 11 floats, 6 externals, b0 b1 a0, then (b, a, d) per dihedral
+        const size_t fbytes = 44 + (size_t)(9 + 3 * nd) * es;
+        const size_t batch = std::max<size_t>(1, (64u << 20) / fbytes);
+        std::vector<unsigned char> buf(batch * fbytes);
+        unsigned char *cols = (unsigned char *)b->cols;
+        unsigned char *B = cols, *A = cols + (size_t)nb * F * es, *Dd = A + (size_t)na * F * es;
+        for (size_t f0 = 0; f0 < F && rc == PG_OK; f0 += batch) {
+            const size_t nf = std::min(batch, F - f0);
+            if (!rd(f, buf.data(), nf * fbytes)) {
+                rc = ioerr(PG_ERR_IO, "An ERROR has occurred while reading the file %s . (frame %zu)", path, f0);
+                break;
+            }
+            // transpose the batch with a few threads (columns are disjoint)
+            const int nth = (int)std::min<size_t>(8, std::max<size_t>(1, nf / 256));
+            auto work = [&](int t) {
+                for (size_t i = t; i < nf; i += nth) {
+                    const unsigned char *p = buf.data() + i * fbytes + 44 + 6 * es;
+                    const size_t fr = f0 + i;
+                    memcpy(B + fr * es, p, es);
+                    memcpy(B + (F + fr) * es, p + es, es);
+                    memcpy(A + fr * es, p + 2 * es, es);
+                    p += 3 * es;
+                    for (int d = 0; d < nd; d++, p += 3 * es) {
+                        memcpy(B + ((size_t)(d + 2) * F + fr) * es, p, es);
+                        memcpy(A + ((size_t)(d + 1) * F + fr) * es, p + es, es);
+                        memcpy(Dd + ((size_t)d * F + fr) * es, p + 2 * es, es);
+                    }
+                }
+            };
+            std::vector<std::thread> th;
+            for (int t = 1; t < nth; t++) th.emplace_back(work, t);
+            work(0);
+            for (auto &x : th) x.join();
+        }
+    } while (0);
+    fclose(f);
+    if (rc != PG_OK) {
+        pg_bat_free(b);
+        return rc;
+    }
+    *out = b;
+    return PG_OK;
+}
+
+PG_API void pg_bat_free(pg_bat *b) {
+    if (!b) return;
+    if (b->cols) {
+        if (b->pinned) cudaFreeHost(b->cols); else free(b->cols);
+    }
+    delete b;
+}
+
+PG_API int pg_bat_view_of(const pg_bat *b, pg_bat_view *v) {
+    if (!b || !v) return PG_ERR_ARG;
+    const size_t F = (size_t)b->h.n_frames, es = b->h.double_prec ? 8 : 4;
+    const int nb = b->h.n_dih + 2, na = b->h.n_dih + 1;
+    v->n_dihedrals = b->h.n_dih;
+    v->n_frames = b->h.n_frames;
+    v->double_prec = b->h.double_prec;
+    v->on_device = 0;
+    v->ld = (int64_t)F;
+    v->bonds = b->cols;
+    v->angles = (const char *)b->cols + (size_t)nb * F * es;
+    v->dihedrals = (const char *)b->cols + (size_t)(nb + na) * F * es;
+    return PG_OK;
+}
+PG_API int pg_bat_n_dihedrals(const pg_bat *b) { return b ? b->h.n_dih : -1; }
+PG_API int pg_bat_n_frames(const pg_bat *b) { return b ? b->h.n_frames : -1; }
+
+PG_API int pg_bat_write_synthetic(const char *path, const pg_bat_view *v) {
+    if (!path || !v || v->on_device || v->n_dihedrals < 0 || v->n_frames < 1 || v->ld < v->n_frames)
+        return ioerr(PG_ERR_ARG, "pg_bat_write_synthetic: bad arguments");
+    FILE *f = fopen(path, "wb");
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: Could not open file %s !", path);
+    Header h;
+    h.version = 3;
+    h.double_prec = v->double_prec;
+    h.n_dih = v->n_dihedrals;
+    h.n_frames = v->n_frames;
+    synthetic_header(h);
+    bool ok = wr(f, &h.version, 4) && wr(f, &h.double_prec, 4) && wr(f, &h.n_dih, 4) && wr(f, &h.n_frames, 4) &&
+              write_atoms(f, h) && (h.n_dih == 0 || wr(f, h.dih.data(), h.dih.size() * 4)) &&
+              wr(f, h.masses.data(), h.masses.size() * 4);
+    const size_t es = v->double_prec ? 8 : 4, nd = (size_t)h.n_dih, ld = (size_t)v->ld;
+    const size_t fbytes = 44 + (9 + 3 * nd) * es;
+    std::vector<unsigned char> fr(fbytes);
+    const unsigned char *B = (const unsigned char *)v->bonds, *A = (const unsigned char *)v->angles,
+                        *Dd = (const unsigned char *)v->dihedrals;
+    for (int t = 0; t < h.n_frames && ok; t++) {
+        memset(fr.data(), 0, 44 + 6 * es);
+        float time = (float)t, prec = 1000.0f;
+        memcpy(fr.data(), &time, 4);
+        memcpy(fr.data() + 4, &prec, 4);
+        unsigned char *p = fr.data() + 44 + 6 * es;
+        memcpy(p, B + (size_t)t * es, es);
+        memcpy(p + es, B + (ld + t) * es, es);
+        memcpy(p + 2 * es, A + (size_t)t * es, es);
+        p += 3 * es;
+        for (size_t d = 0; d < nd; d++, p += 3 * es) {
+            memcpy(p, B + ((d + 2) * ld + t) * es, es);
+            memcpy(p + es, A + ((d + 1) * ld + t) * es, es);
+            memcpy(p + 2 * es, Dd + (d * ld + t) * es, es);
+        }
+        ok = wr(f, fr.data(), fbytes);
+    }
+    if (fclose(f) != 0) ok = false;
+    return ok ? PG_OK : ioerr(PG_ERR_IO, "AN ERROR HAS OCCURED WHILE WRITING THE FILE %s", path);
+}
+
+PG_API int pg_par_write(const char *path, const pg_bat *b, const int bins[6], const pg_par_body *body) {
+    if (!path || !b || !bins || !body) return ioerr(PG_ERR_ARG, "pg_par_write: null argument");
+    FILE *f = fopen(path, "wb");
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: Could not open file %s !", path);
+    const Header &h = b->h;
+    const int version = 4;
+    bool ok = wr(f, &version, 4) && wr(f, &h.double_prec, 4) && wr(f, &h.n_dih, 4) && wr(f, &h.n_frames, 4);
+    for (int k = 0; k < 6 && ok; k++) ok = wr(f, &bins[k], 4);  // b1D a1D d1D b2D a2D d2D
+    ok = ok && write_atoms(f, h) && (h.n_dih == 0 || wr(f, h.dih.data(), h.dih.size() * 4)) &&
+         wr(f, h.masses.data(), h.masses.size() * 4);
+    int64_t off[10];
+    layout(h.n_dih, off);
+    const double *src[9] = {body->s1_b, body->s1_a, body->s1_d, body->bb, body->ba, body->bd, body->aa, body->ad, body->dd};
+    for (int k = 0; k < 9 && ok; k++) {
+        const int64_t n = off[k + 1] - off[k];
+        if (n > 0) ok = src[k] && wr(f, src[k], (size_t)n * 8);
+    }
+    if (fclose(f) != 0) ok = false;
+    return ok ? PG_OK : ioerr(PG_ERR_IO, "AN ERROR HAS OCCURED WHILE WRITING THE FILE %s .", path);
+}
+
+PG_API int pg_par_read(const char *path, pg_par **out) {
+    if (!path || !out) return ioerr(PG_ERR_ARG, "pg_par_read: null argument");
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: COULD NOT OPEN FILE %s !", path);
+    pg_par *p = new pg_par;
+    Header &h = p->h;
+    int rc = PG_OK;
+    do {
+        int hv[4];
+        if (!rd(f, hv, 16) || !rd(f, p->bins, 24)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
+        h.version = hv[0]; h.double_prec = hv[1]; h.n_dih = hv[2]; h.n_frames = hv[3];
+        // the checks of read_PAR_header, io_binary.cpp:477-519
+        if (h.version < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version); break; }
+        if (h.double_prec != 0 && h.double_prec != 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!", h.double_prec); break; }
+        if (h.n_dih > 19997) fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n", h.n_dih + 3);
+        if (h.n_dih < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih); break; }
+        if (h.n_frames < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames); break; }
+        static const char *nm[6] = {"BONDS IN 1D", "ANGLES IN 1D", "DIHEDRALS IN 1D", "BONDS IN 2D", "ANGLES IN 2D", "DIHEDRALS IN 2D"};
+        for (int k = 0; k < 6 && rc == PG_OK; k++)
+            if (p->bins[k] < 1) rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER BINS FOR %s (%d) < 1!", nm[k], p->bins[k]);
+        if (rc) break;
+        if (h.version >= 3) {
+            if (!read_atoms(f, h)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
+        } else {
+            synthetic_header(h);
+        }
+        h.dih.resize((size_t)6 * h.n_dih);
+        for (int i = 0; i < h.n_dih && rc == PG_OK; i++) {  // io_binary.cpp:554-596
+            if (!rd(f, &h.dih[6 * i], 24)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
+            for (int k = 0; k < 4; k++)
+                if (h.dih[6 * i + k] < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL ID < 1 !"); break; }
+            if (rc) break;
+            const int ty = h.dih[6 * i + 4];
+            if (!(ty == 1 || ty == 0 || ty == -1)) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL TYPE NEITHER 0, 1 NOR -1 !"); break; }
+            if (h.dih[6 * i + 5] < -1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL IS PHASEANGLE OF A DIHEDRAL WITH NEGATIVE ID !"); break; }
+            if (h.version == 1 && h.dih[6 * i + 5] != -1) h.dih[6 * i + 5]++;
+        }
+        if (rc) break;
+        h.masses.resize((size_t)h.n_dih + 3);
+        if (!rd(f, h.masses.data(), h.masses.size() * 4)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
+        layout(h.n_dih, p->off);
+        try {
+            p->body.resize((size_t)p->off[9]);
+        } catch (...) {
+            rc = ioerr(PG_ERR_NOMEM, "ERROR: ALLOCATION FOR PAR FILE BODY FAILED. MORE MEMORY NEEDED?");
+            break;
+        }
+        if (p->off[9] && !rd(f, p->body.data(), (size_t)p->off[9] * 8)) { rc = ioerr(PG_ERR_IO, "ERROR READING FILE %s !", path); break; }
+    } while (0);
+    fclose(f);
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return PG_OK;
+}
+
+PG_API void pg_par_free(pg_par *p) { delete p; }
+PG_API int pg_par_n_dihedrals(const pg_par *p) { return p ? p->h.n_dih : -1; }
+PG_API int pg_par_bins(const pg_par *p, int bins[6]) {
+    if (!p || !bins) return PG_ERR_ARG;
+    memcpy(bins, p->bins, sizeof p->bins);
+    return PG_OK;
+}
+PG_API int pg_par_body_of(const pg_par *p, pg_par_body *b) {
+    if (!p || !b) return PG_ERR_ARG;
+    double *base = const_cast<double *>(p->body.data());
+    double **dst[9] = {&b->s1_b, &b->s1_a, &b->s1_d, &b->bb, &b->ba, &b->bd, &b->aa, &b->ad, &b->dd};
+    for (int k = 0; k < 9; k++) *dst[k] = base + p->off[k];
+    return PG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ text
+
+namespace {
+
+// Buffered writer; doubles as C++ ostream precision(12) prints them (%.12g).
+struct Out {
+    FILE *f;
+    std::vector<char> buf;
+    size_t n = 0;
+    explicit Out(FILE *fp) : f(fp), buf(1 << 22) {}
+    void flush() {
+        if (n) fwrite(buf.data(), 1, n, f);
+        n = 0;
+    }
+    void room(size_t k) {
+        if (n + k > buf.size()) flush();
+    }
+    Out &s(const char *t) {
+        size_t k = strlen(t);
+        room(k);
+        memcpy(buf.data() + n, t, k);
+        n += k;
+        return *this;
+    }
+    Out &i(long long v) {
+        room(32);
+        n += (size_t)snprintf(buf.data() + n, 32, "%lld", v);
+        return *this;
+    }
+    Out &d(double v) {
+        room(40);
+        n += (size_t)snprintf(buf.data() + n, 40, "%.12g", v);
+        return *this;
+    }
+    ~Out() { flush(); }
+};
+
+double mutual(int type, int i1, int i2, int nd_, const pg_par_body *b) {  // util.cpp:47-81
+    const int nb = nd_ + 2, na = nd_ + 1, nd = nd_;
+    const int s = i1 < i2 ? i1 : i2, g = i1 < i2 ? i2 : i1;
+    switch (type) {
+    case 0: if (i1 == i2) break; return b->s1_b[s] + b->s1_b[g] - b->bb[(int64_t)(nb - s) * (nb - s - 1) / 2 + s - g];
+    case 1: return b->s1_b[i1] + b->s1_a[i2] - b->ba[(int64_t)i1 * na + i2];
+    case 2: return b->s1_b[i1] + b->s1_d[i2] - b->bd[(int64_t)i1 * nd + i2];
+    case 3: if (i1 == i2) break; return b->s1_a[s] + b->s1_a[g] - b->aa[(int64_t)(na - s) * (na - s - 1) / 2 + s - g];
+    case 4: return b->s1_a[i1] + b->s1_d[i2] - b->ad[(int64_t)i1 * nd + i2];
+    case 5: if (i1 == i2) break; return b->s1_d[s] + b->s1_d[g] - b->dd[(int64_t)(nd - s) * (nd - s - 1) / 2 + s - g];
+    }
+    fprintf(stderr, "WARNING: REQUEST FOR MUTUAL INFORMATION TYPE %d WITH INDICES %d AND %dYIELDED NO RESULT.\n", type, i1, i2);
+    return 0;
+}
+
+FILE *open_out(const char *path) { return path ? fopen(path, "w") : stdout; }
+int close_out(const char *path, FILE *f) { return path ? (fclose(f) == 0 ? PG_OK : PG_ERR_IO) : (fflush(f), PG_OK); }
+
+}  // namespace
+
+extern "C" {
+
+PG_API int pg_write_mie_text(const char *path, int n_dih, const pg_par_body *b) {
+    if (!b || n_dih < 0) return ioerr(PG_ERR_ARG, "pg_write_mie_text: bad arguments");
+    FILE *f = open_out(path);
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: COULD NOT OPEN FILE %s !", path);
+    {
+        Out o(f);
+        const int nb = n_dih + 2, na = n_dih + 1, nd = n_dih;
+        double tB = 0, tA = 0, tD = 0, e[6] = {0}, m[6] = {0};
+        for (int k = 0; k < nb; k++) { o.s("bond ").i(k + 1).s("   ").d(b->s1_b[k]).s("\n"); tB += b->s1_b[k]; }
+        for (int k = 0; k < na; k++) { o.s("angle ").i(k + 1).s("   ").d(b->s1_a[k]).s("\n"); tA += b->s1_a[k]; }
+        for (int k = 0; k < nd; k++) { o.s("dihedral ").i(k + 1).s("   ").d(b->s1_d[k]).s("\n"); tD += b->s1_d[k]; }
+        const char *nm[6] = {"bond-bond ", "bond-angle ", "bond-dihedral ", "angle-angle ", "angle-dihedral ", "dihedral-dihedral "};
+        const int n1[6] = {nb, nb, nb, na, na, nd}, n2[6] = {nb, na, nd, na, nd, nd};
+        const double *blk[6] = {b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
+        for (int q = 0; q < 6; q++) {
+            const bool same = q == 0 || q == 3 || q == 5;
+            int64_t counter = (int64_t)n1[q] * (n1[q] - 1) / 2 - 1;
+            for (int i = 0; i < (same ? n1[q] - 1 : n1[q]); i++)
+                for (int j = same ? i + 1 : 0; j < n2[q]; j++) {
+                    const double mu = mutual(q, i, j, n_dih, b);
+                    const double s2 = same ? blk[q][counter--] : blk[q][(int64_t)i * n2[q] + j];
+                    o.s(nm[q]).i(i + 1).s("  ").i(j + 1).s("   ").d(s2).s("   ").d(mu).s("\n");
+                    e[q] += s2;
+                    m[q] += mu;
+                }
+        }
+        o.s("TOTAL 1D BONDS ENTROPY = ").d(tB).s("\n");
+        o.s("TOTAL 1D ANGLES ENTROPY = ").d(tA).s("\n");
+        o.s("TOTAL 1D DIHEDRALS ENTROPY = ").d(tD).s("\n");
+        const char *tn[6] = {"BONDS-BONDS", "BONDS-ANGLES", "BONDS-DIHEDRALS", "ANGLES-ANGLES", "ANGLES-DIHEDRALS", "DIHEDRALS-DIHEDRALS"};
+        for (int q = 0; q < 6; q++) {
+            o.s("TOTAL 2D ").s(tn[q]).s(" ENTROPY = ").d(e[q]).s("\n");
+            o.s("TOTAL 2D ").s(tn[q]).s(" MUTUAL INFORMATION = ").d(m[q]).s("\n");
+        }
+        o.s("TOTAL CONFIGURATIONAL ENTROPY = ").d(tB + tA + tD - m[0] - m[1] - m[2] - m[3] - m[4] - m[5]).s("\n");
+    }
+    return close_out(path, f);
+}
+
+PG_API int pg_write_mist_text(const char *path, int n_dih, const pg_mist_edge *edges, const double totals[10]) {
+    if (!edges || !totals || n_dih < 0) return ioerr(PG_ERR_ARG, "pg_write_mist_text: bad arguments");
+    FILE *f = open_out(path);
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: COULD NOT OPEN FILE %s !", path);
+    {
+        Out o(f);
+        const char ch[3] = {'b', 'a', 'd'};
+        const int n = 3 * n_dih + 3 - 1;
+        for (int s = 0; s < n; s++) {
+            const char t[5] = {ch[edges[s].type_in], ' ', ch[edges[s].type_out], ' ', 0};
+            o.s(t).i(edges[s].index_in).s(" ").i(edges[s].index_out).s("   MI: ").d(edges[s].mi).s("   left to process: ").i(edges[s].left).s("\n");
+        }
+        const char *lines[10] = {"TOTAL 1D BONDS ENTROPY = ", "TOTAL 1D ANGLES ENTROPY = ", "TOTAL 1D DIHEDRALS ENTROPY = ",
+                                 "TOTAL 2D BONDS-BONDS MUTUAL INFORMATION = ", "TOTAL 2D BONDS-ANGLES MUTUAL INFORMATION = ",
+                                 "TOTAL 2D BONDS-DIHEDRALS MUTUAL INFORMATION = ", "TOTAL 2D ANGLES-ANGLES MUTUAL INFORMATION = ",
+                                 "TOTAL 2D ANGLES-DIHEDRALS MUTUAL INFORMATION = ", "TOTAL 2D DIHEDRALS-DIHEDRALS MUTUAL INFORMATION = ",
+                                 "TOTAL CONFIGURATIONAL ENTROPY = "};
+        for (int k = 0; k < 10; k++) o.s(lines[k]).d(totals[k]).s("\n");
+    }
+    return close_out(path, f);
+}
+
+PG_API int pg_write_info_text(const char *path, const pg_par *p) {
+    if (!p) return ioerr(PG_ERR_ARG, "pg_write_info_text: null argument");
+    const Header &h = p->h;
+    if (h.n_dih < 1) return ioerr(PG_ERR_ARG, "pg_write_info_text: no dihedrals");
+    FILE *f = open_out(path);
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: COULD NOT OPEN FILE %s !", path);
+    {
+        Out o(f);
+        const int *d = h.dih.data();
+        o.s("#bond #atom1 #atom2 \n");
+        o.s("1 ").i(d[0]).s(" ").i(d[1]).s("\n");
+        o.s("2 ").i(d[1]).s(" ").i(d[2]).s("\n");
+        for (int i = 0; i < h.n_dih; i++) o.i(i + 3).s(" ").i(d[6 * i + 2]).s(" ").i(d[6 * i + 3]).s("\n");
+        o.s("#angle #atom1 #atom2 #atom3\n");
+        o.s("1 ").i(d[0]).s(" ").i(d[1]).s(" ").i(d[2]).s("\n");
+        for (int i = 0; i < h.n_dih; i++) o.i(i + 2).s(" ").i(d[6 * i + 1]).s(" ").i(d[6 * i + 2]).s(" ").i(d[6 * i + 3]).s("\n");
+        o.s("#dihedral #atom1 #atom2 #atom3 #atom4    dihedral_type(common=0,pseudo=1,improper=-1)   phaseangle_of(-1 if no phaseangle)\n");
+        for (int i = 0; i < h.n_dih; i++)
+            o.i(i + 1).s(" ").i(d[6 * i]).s(" ").i(d[6 * i + 1]).s(" ").i(d[6 * i + 2]).s(" ").i(d[6 * i + 3]).s(" ").i(d[6 * i + 4]).s(" ").i(d[6 * i + 5]).s("\n");
+    }
+    return close_out(path, f);
+}
+
+}  // extern "C"

@@ -1,0 +1,271 @@
+// Per-DOF preprocessing: one CTA per DOF.
+//   pass 1 (dihedrals only): 100-bin occupancy histogram and the "modfit"
+//           shift that moves the longest empty stretch to 2 pi (PARENT.cpp:564-612)
+//   pass 2: extrema of the (shifted) column, padding and clamps (PARENT.cpp:511-636)
+//   pass 3: uint8 bin index at the 2D bin count for every frame (the pair
+//           kernels' input), 1D histogram at the 1D bin count and the marginal
+//           at the 2D bin count; then the 1D entropy (PARENT.cpp:650-757) and the
+//           per-DOF constant A of the 2D entropy decomposition.
+//
+// Bit-exactness: every FP64 operation that decides a bin index is written
+// with explicit round-to-nearest intrinsics (no FMA contraction), and this
+// file is compiled with --fmad=false, so bin indices equal the reference's
+// int((x - min) / binsize) on x86-64 (which never fuses).
+#include <math.h>
+
+#include "pg_internal.h"
+
+namespace pg {
+
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kModfitBins = 100;  // PARENT.cpp:51
+
+__device__ __forceinline__ double load_val(const void *col, int prec, int64_t f) {
+    return prec ? __ldg((const double *)col + f) : (double)__ldg((const float *)col + f);
+}
+
+// x + modFit - 2 pi int((x + modFit) / (2 pi)), PARENT.cpp:611, evaluated as
+// the reference's left-to-right expression without contraction.
+__device__ __forceinline__ double shifted(double x, double modfit, double twopi) {
+    const double t = __dadd_rn(x, modfit);
+    const int q = __double2int_rz(__ddiv_rn(t, twopi));
+    return __dsub_rn(t, __dmul_rn(twopi, (double)q));
+}
+
+__device__ __forceinline__ int bin_index(double x, double mn, double bs) {
+    return __double2int_rz(__ddiv_rn(__dsub_rn(x, mn), bs));
+}
+
+__global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb,
+                                                        const void *ca, const void *cd,
+                                                        int64_t ld, int prec, DofArrays dof,
+                                                        uint8_t *bins, int *err,
+                                                        double modfit_bs, double pi) {
+    extern __shared__ unsigned int sh[];
+    const int g = blockIdx.x;
+    const int type = dof_type(g, geo.nb, geo.na);
+    const int local = g - (type == TB ? 0 : (type == TA ? geo.nb : geo.nb + geo.na));
+    const void *col = type == TB ? cb : (type == TA ? ca : cd);
+    col = prec ? (const void *)((const double *)col + (int64_t)local * ld)
+               : (const void *)((const float *)col + (int64_t)local * ld);
+    const int F = geo.F;
+    const int B1 = geo.bins[type], B2 = geo.bins[3 + type];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const double twopi = 2 * pi;
+
+    // shared layout: [kWarps][kModfitBins] | [kWarps][B1] | [kWarps][B2] | scalars
+    unsigned int *hmod = sh;
+    unsigned int *h1 = hmod + kWarps * kModfitBins;
+    unsigned int *h2 = h1 + kWarps * B1;
+    __shared__ double s_shift, s_mn, s_mx;
+    __shared__ double red_mn[kWarps], red_mx[kWarps];
+
+    double modfit = 0.0;
+    if (type == TD) {
+        for (int k = tid; k < kWarps * kModfitBins; k += kThreads) hmod[k] = 0;
+        __syncthreads();
+        int bad = 0;
+        for (int f = tid; f < F; f += kThreads) {
+            int idx = __double2int_rz(__ddiv_rn(load_val(col, prec, f), modfit_bs));
+            if (idx < 0 || idx >= kModfitBins) { bad++; idx = idx < 0 ? 0 : kModfitBins - 1; }
+            atomicAdd(&hmod[warp * kModfitBins + idx], 1u);
+        }
+        if (bad) atomicAdd(&err[ERR_MODFIT_RANGE], bad);
+        __syncthreads();
+        for (int k = tid; k < kModfitBins; k += kThreads) {
+            unsigned int s = 0;
+            for (int w = 0; w < kWarps; w++) s += hmod[w * kModfitBins + k];
+            hmod[k] = s;  // warp 0's row only read by thread k itself before this write
+        }
+        __syncthreads();
+        if (tid == 0) {
+            // longest circular stretch of empty bins, or the first minimum bin
+            // when none is empty (PARENT.cpp:573-608, including the run
+            // counter that starts at 2 because of the double increment)
+            const unsigned int *histo = hmod;
+            bool zeroExists = false;
+            for (int k = 0; k < kModfitBins; k++) zeroExists = zeroExists || (histo[k] == 0);
+            int longest = 0, longestPos = -1, cur = 0, curPos = 0;
+            if (zeroExists) {
+                for (int k = 0; k < 2 * kModfitBins; k++) {
+                    const int l = k % kModfitBins;
+                    if (cur == 0 && histo[l] == 0) { cur = 1; curPos = k; }
+                    if (cur > 0 && histo[l] == 0) cur += 1;
+                    if (cur > 0 && histo[l] != 0) {
+                        if (cur > longest) { longest = cur; longestPos = curPos; }
+                        cur = 0;
+                    }
+                }
+            } else {
+                longestPos = 0;
+                unsigned int mn = histo[0];
+                for (int k = 0; k < kModfitBins; k++)
+                    if (histo[k] < mn) { mn = histo[k]; longestPos = k; }
+            }
+            // modFit = 2 pi - (pos + 0.5) * binsize, PARENT.cpp:609
+            s_shift = __dsub_rn(twopi, __dmul_rn(__dadd_rn((double)longestPos, 0.5), modfit_bs));
+        }
+        __syncthreads();
+        modfit = s_shift;
+    }
+
+    // ---- extrema (PARENT.cpp:512-521, 539-548, 614-623)
+    double lmax = -1.0e100, lmin = 1.0e100;
+    for (int f = tid; f < F; f += kThreads) {
+        double x = load_val(col, prec, f);
+        if (type == TD) x = shifted(x, modfit, twopi);
+        if (x > lmax) lmax = x;
+        if (x < lmin) lmin = x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double a = __shfl_xor_sync(0xffffffffu, lmax, o);
+        const double b = __shfl_xor_sync(0xffffffffu, lmin, o);
+        if (a > lmax) lmax = a;
+        if (b < lmin) lmin = b;
+    }
+    if (lane == 0) { red_mx[warp] = lmax; red_mn[warp] = lmin; }
+    __syncthreads();
+    if (tid == 0) {
+        double tmpMax = -1.0e100, tmpMin = 1.0e100;
+        for (int w = 0; w < kWarps; w++) {
+            if (red_mx[w] > tmpMax) tmpMax = red_mx[w];
+            if (red_mn[w] < tmpMin) tmpMin = red_mn[w];
+        }
+        if (type == TB && ((tmpMin < 0.0) || (tmpMax < 0.0))) atomicAdd(&err[ERR_NEG_BOND], 1);
+        tmpMin = __dsub_rn(tmpMin, 0.000000005);
+        tmpMax = __dadd_rn(tmpMax, 0.000000005);
+        if (tmpMin < 0.0) tmpMin = 0.0;
+        if (type == TA && tmpMax > pi) tmpMax = pi;
+        if (type == TD && tmpMax > twopi) tmpMax = twopi;
+        if (__dsub_rn(tmpMax, tmpMin) < 1.0e-4) tmpMax = __dadd_rn(tmpMax, 0.05);
+        s_mn = tmpMin;
+        s_mx = tmpMax;
+        dof.mn[g] = tmpMin;
+        dof.mx[g] = tmpMax;
+        dof.shift[g] = modfit;
+        dof.b2[g] = B2;
+    }
+    for (int k = tid; k < kWarps * (B1 + B2); k += kThreads) h1[k] = 0;
+    __syncthreads();
+
+    // ---- binning (PARENT.cpp:654-656 1D; :800-803 and the other 2D fills)
+    const double mn = s_mn, mx = s_mx;
+    const double bs1 = __ddiv_rn(__dsub_rn(mx, mn), (double)B1);
+    const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
+    uint8_t *brow = bins + (int64_t)g * geo.ldb;
+    int bad = 0;
+    for (int f = tid; f < F; f += kThreads) {
+        double x = load_val(col, prec, f);
+        if (type == TD) x = shifted(x, modfit, twopi);
+        int i1 = bin_index(x, mn, bs1);
+        int i2 = bin_index(x, mn, bs2);
+        if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
+        if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
+        atomicAdd(&h1[warp * B1 + i1], 1u);
+        atomicAdd(&h2[warp * B2 + i2], 1u);
+        brow[f] = (uint8_t)i2;
+    }
+    if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);
+    __syncthreads();
+    for (int k = tid; k < B1 + B2; k += kThreads) {
+        unsigned int *h = k < B1 ? h1 : h2;
+        const int kk = k < B1 ? k : k - B1, stride = k < B1 ? B1 : B2;
+        unsigned int s = 0;
+        for (int w = 0; w < kWarps; w++) s += h[w * stride + kk];
+        h[kk] = s;
+    }
+    __syncthreads();
+
+    if (tid == 0) {
+        // 1D entropy in the reference's order (PARENT.cpp:658-670, 702-714, 746-756)
+        const int N = F;
+        int occupbins = 0;
+        double plnpsum = 0.0, probDens;
+        if (type == TB) {
+            double blen = __dadd_rn(mn, bs1 / 2.0);
+            for (int k = 0; k < B1; k++) {
+                probDens = (double)h1[k] / (((N * bs1) * blen) * blen);
+                if (probDens > 0) {
+                    plnpsum = plnpsum + ((blen * blen) * probDens) * log(probDens);
+                    occupbins++;
+                }
+                blen = __dadd_rn(blen, bs1);
+            }
+        } else if (type == TA) {
+            double theta = __dadd_rn(mn, bs1 / 2.0);
+            for (int k = 0; k < B1; k++) {
+                const double st = sin(theta);
+                probDens = (double)h1[k] / ((N * bs1) * st);
+                if (probDens > 0) {
+                    plnpsum = plnpsum + (st * probDens) * log(probDens);
+                    occupbins++;
+                }
+                theta = __dadd_rn(theta, bs1);
+            }
+        } else {
+            for (int k = 0; k < B1; k++) {
+                probDens = (double)h1[k] / (N * bs1);
+                if (probDens > 0) {
+                    plnpsum = plnpsum + probDens * log(probDens);
+                    occupbins++;
+                }
+            }
+        }
+        plnpsum = -plnpsum * bs1;
+        dof.s1[g] = plnpsum + (occupbins - 1.0) / (2.0 * N);
+
+        // A = ln(bs2) + (1/N) sum_k m(k) ln J(c_k), with c_k advanced by
+        // repeated += binsize as the reference's 2D epilogues do
+        // (e.g. PARENT.cpp:807-820); J = c^2 (bond), sin c (angle), 1 (dihedral).
+        double acc = 0.0;
+        if (type != TD) {
+            double c = __dadd_rn(mn, bs2 / 2.0);
+            for (int k = 0; k < B2; k++) {
+                if (h2[k]) acc += (double)h2[k] * (type == TB ? log(c * c) : log(sin(c)));
+                c = __dadd_rn(c, bs2);
+            }
+        }
+        dof.acon[g] = log(bs2) + acc / (double)N;
+    }
+}
+
+__global__ void nlogn_kernel(double *t, int nmax) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
+        t[n] = n > 1 ? (double)n * log((double)n) : 0.0;
+}
+
+}  // namespace
+
+cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st) {
+    int blocks = (nmax + 1 + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    nlogn_kernel<<<blocks, 256, 0, st>>>(nlogn, nmax);
+    return cudaGetLastError();
+}
+
+size_t prep_smem_bytes(const SysGeom &g) {
+    int m1 = 0, m2 = 0;
+    for (int t = 0; t < 3; t++) {
+        if (g.bins[t] > m1) m1 = g.bins[t];
+        if (g.bins[3 + t] > m2) m2 = g.bins[3 + t];
+    }
+    return (size_t)kWarps * (kModfitBins + m1 + m2) * sizeof(unsigned int);
+}
+
+cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
+                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st) {
+    const double pi = acos(-1.0);  // PARENT.cpp:112
+    const double modfit_bs = (2 * pi + 0.000000005) / kModfitBins;  // PARENT.cpp:569
+    const size_t smem = prep_smem_bytes(g);
+    cudaError_t e = cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    prep_kernel<<<g.D, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof,
+                                             bins, err, modfit_bs, pi);
+    return cudaGetLastError();
+}
+
+}  // namespace pg

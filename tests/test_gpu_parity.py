@@ -1,0 +1,288 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's own outputs.
+
+Bars: bin-decision inputs (per-DOF min/max/shift) and every 2D histogram
+count bit-exact; 1D/2D entropies and MI within 1e-9 nats of the FP64
+oracle (the BASELINE bar is 1e-5 nats; the decomposition error is ~1e-12);
+MIST edge list identical (types, indices, order), MI of each edge within
+1e-9, totals within 1e-7.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+import parent_gb300 as pg
+from conftest import FIXTURES, GOLDEN, par_body_from_file, read_text_gz
+
+pytestmark = pytest.mark.gpu
+
+S_TOL = 1e-9      # nats, entropies
+MI_TOL = 1e-5     # nats, the BASELINE bar for every MI term
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = pg.Engine(0)
+    yield e
+    e.close()
+
+
+def mutual_all(n: int, body: dict) -> np.ndarray:
+    """Every pair's MI as get_mutual (util.cpp:47-81) forms it, in body order."""
+    nb, na, nd = n + 2, n + 1, n
+    s1b, s1a, s1d = body["s1_b"], body["s1_a"], body["s1_d"]
+    out = []
+    for key, s1, m in (("bb", s1b, nb), ("aa", s1a, na), ("dd", s1d, nd)):
+        if m < 2:
+            continue
+        i, j = np.triu_indices(m, 1)          # lexicographic
+        mi = s1[i] + s1[j] - body[key][::-1]  # stored reversed
+        out.append(mi)
+    for key, s1, s2 in (("ba", s1b, s1a), ("bd", s1b, s1d), ("ad", s1a, s1d)):
+        if s2.size == 0:
+            continue
+        out.append((s1[:, None] + s2[None, :]).ravel() - body[key])
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+def compare_bodies(n, gpu: pg.ParBody, ref: dict, s_tol=S_TOL):
+    for k in oracle.BLOCKS:
+        a, b = gpu.blocks[k], ref[k]
+        assert a.shape == b.shape, k
+        if a.size:
+            err = np.max(np.abs(a - b))
+            assert err <= s_tol, f"{k}: max |dS| = {err:.3e}"
+    dmi = np.abs(mutual_all(n, gpu.blocks) - mutual_all(n, ref))
+    if dmi.size:
+        assert dmi.max() <= MI_TOL
+    return float(dmi.max()) if dmi.size else 0.0
+
+
+def compare_mist(gpu_edges, gpu_tot, ref_edges, ref_tot):
+    for f in ("t1", "t2", "i1", "i2", "left"):
+        assert np.array_equal(gpu_edges[f], ref_edges[f]), f
+    assert np.max(np.abs(gpu_edges["mi"] - ref_edges["mi"]), initial=0.0) <= S_TOL
+    assert np.max(np.abs(gpu_tot - ref_tot)) <= 1e-7
+
+
+def parse_mist_text(lines):
+    ch = {"b": 0, "a": 1, "d": 2}
+    edges = []
+    for ln in lines:
+        if ln.startswith("TOTAL"):
+            break
+        p = ln.split()
+        edges.append((ch[p[0]], ch[p[1]], int(p[2]), int(p[3]), float(p[5]), int(p[9])))
+    arr = np.array(edges, dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"), ("left", "i4")])
+    tot = np.array([float(ln.split(" = ")[1]) for ln in lines if ln.startswith("TOTAL")])
+    return arr, tot
+
+
+# ------------------------------------------------------------ golden fixtures
+
+@pytest.mark.parametrize("stem", FIXTURES)
+def test_fixture_par_matches_reference(eng, stem):
+    bat = pg.BatFile(GOLDEN / f"{stem}.bat")
+    body = eng.entropy(bat.view(), (50,) * 6, "hist")
+    n, ref = par_body_from_file(GOLDEN / f"{stem}_ref.par")
+    compare_bodies(n, body, ref)
+    # MIST on the MI matrix left resident on the device
+    e, t = eng.mist(n)
+    re, rt = parse_mist_text(read_text_gz(f"{stem}_ref_MIST.txt.gz"))
+    for f in ("t1", "t2", "i1", "i2", "left"):
+        assert np.array_equal(e[f], re[f]), f
+    assert np.max(np.abs(e["mi"] - re["mi"])) <= 1e-9
+    assert np.max(np.abs(t - rt) / np.maximum(1.0, np.abs(rt))) <= 1e-10
+
+
+@pytest.mark.parametrize("stem", FIXTURES)
+def test_fixture_mist_from_reference_par(eng, stem):
+    """get_PAR_MIST on the reference's own .par: edges and text identical."""
+    p = pg.ParFile(GOLDEN / f"{stem}_ref.par")
+    e, t = eng.mist(p.n_dih, p.body)
+    re, rt = oracle.mist(p.n_dih, p.body.blocks)
+    compare_mist(e, t, re, rt)
+    lines = []
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as d:
+        pg.write_mist_text(os.path.join(d, "m.txt"), p.n_dih, e, t)
+        lines = open(os.path.join(d, "m.txt")).read().splitlines()
+    assert lines == read_text_gz(f"{stem}_ref_MIST.txt.gz")
+
+
+@pytest.mark.parametrize("stem", FIXTURES)
+def test_fixture_counts_and_stats_bit_exact(eng, stem):
+    n, F, prec, b, a, d = oracle.read_bat(GOLDEN / f"{stem}.bat")
+    bat = pg.BatFile(GOLDEN / f"{stem}.bat")
+    D = 3 * n + 3
+    rng = np.random.default_rng(7)
+    pairs = sorted({tuple(sorted(rng.choice(D, 2, replace=False).tolist())) for _ in range(60)})
+    pairs += [(0, 1), (0, D - 1), (D - 2, D - 1), (n + 1, n + 2)]
+    traj = pg.Trajectory(*(np.ascontiguousarray(x.astype(np.float64 if prec else np.float32)) for x in (b, a, d)))
+    got = eng.pair_counts(traj, (50,) * 6, pairs)
+    want = oracle.pair_counts(b, a, d, (50,) * 6, pairs)
+    for (g1, g2), x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), (g1, g2)
+    mn, mx, sh = eng.dof_stats(D)
+    omn, omx, osh, _, bad = oracle.extrema(b, a, d)
+    assert bad == 0
+    assert np.array_equal(mn.view(np.uint64), omn.view(np.uint64))
+    assert np.array_equal(mx.view(np.uint64), omx.view(np.uint64))
+    assert np.array_equal(sh.view(np.uint64), osh.view(np.uint64))
+
+
+# ------------------------------------------------------------ synthetic systems
+
+def _synth_case(n_atoms, F, prec, seed, **kw):
+    return pg.synth_host(n_atoms, F, double_prec=prec, seed=seed, **kw)
+
+
+@pytest.mark.parametrize("n_atoms,F,prec,bins", [
+    (100, 20000, 1, (50,) * 6),                      # the CPU-runnable config shape (294 DOFs, FP64)
+    (40, 12345, 0, (50,) * 6),                       # FP32, ragged frame count
+    (30, 5000, 0, (7, 64, 100, 10, 20, 30)),         # different bin counts per type
+    (25, 3000, 1, (1, 1, 1, 1, 1, 1)),               # one bin
+    (3, 777, 1, (50,) * 6),                          # no dihedrals
+    (4, 1, 1, (50,) * 6),                            # one frame: constant columns
+    (12, 4096, 0, (50, 50, 50, 100, 100, 100)),      # 2x2 tile kernel
+    (9, 2000, 1, (50, 50, 50, 200, 180, 150)),       # 1x1 tile kernel
+])
+def test_synthetic_matches_oracle(eng, n_atoms, F, prec, bins):
+    t = _synth_case(n_atoms, F, prec, seed=n_atoms * 7 + F, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05)
+    body = eng.entropy(t, bins, "hist")
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    n = n_atoms - 3
+    compare_bodies(n, body, ref)
+    e, tot = eng.mist(n)
+    re, rt = oracle.mist(n, ref)
+    compare_mist(e, tot, re, rt)
+
+
+def test_counts_bit_exact_mixed_bins(eng):
+    t = _synth_case(30, 9000, 0, seed=5, frac_bimodal_dih=0.3)
+    bins = (13, 50, 77, 17, 33, 50)
+    D = 3 * 27 + 3
+    pairs = [(i, j) for i in range(0, D, 7) for j in range(i + 1, D, 5)]
+    got = eng.pair_counts(t, bins, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, bins, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
+
+
+def test_form_auto_and_hist_agree(eng):
+    t = _synth_case(20, 3000, 1, seed=11)
+    a = eng.entropy(t, (50,) * 6, "auto").flat()
+    b = eng.entropy(t, (50,) * 6, "hist").flat()
+    assert np.max(np.abs(a - b)) <= S_TOL
+
+
+def test_repeat_is_deterministic(eng):
+    t = _synth_case(50, 10000, 0, seed=3)
+    a = eng.entropy(t, (50,) * 6, "hist").flat()
+    b = eng.entropy(t, (50,) * 6, "hist").flat()
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+# ------------------------------------------------------------ MIST ties
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_mist_tie_order_matches_reference_scan(eng, seed):
+    """Quantised MI values make many exact ties; the GPU tree must follow the
+    reference's first-maximum scan order (get_PAR_MIST.cpp:481-606)."""
+    n = 20
+    rng = np.random.default_rng(seed)
+    body = {k: np.round(rng.normal(0, 2, s) * 2) / 2 for k, s in oracle.sizes(n).items()}
+    for k in ("s1_b", "s1_a", "s1_d"):
+        body[k] = np.round(rng.normal(0, 1, oracle.sizes(n)[k]) * 4) / 4
+    pb = pg.ParBody(n, {k: np.ascontiguousarray(v) for k, v in body.items()})
+    e, t = eng.mist(n, pb)
+    re, rt = oracle.mist(n, body)
+    compare_mist(e, t, re, rt)
+
+
+# ------------------------------------------------------------ error paths
+
+def test_negative_bond_is_rejected(eng):
+    t = _synth_case(10, 500, 1, seed=1)
+    t.bonds[3, 17] = -0.1
+    with pytest.raises(pg.PGError) as e:
+        eng.entropy(t, (50,) * 6, "hist")
+    assert e.value.code == pg.PG_ERR_DATA
+
+
+def test_dihedral_outside_shift_histogram_is_rejected(eng):
+    t = _synth_case(10, 500, 1, seed=1)
+    t.dihedrals[2, 5] = 7.0
+    with pytest.raises(pg.PGError) as e:
+        eng.entropy(t, (50,) * 6, "hist")
+    assert e.value.code == pg.PG_ERR_DATA
+
+
+@pytest.mark.parametrize("bins,code", [((50, 50, 50, 50, 50, 0), pg.PG_ERR_ARG),
+                                       ((0, 50, 50, 50, 50, 50), pg.PG_ERR_ARG),
+                                       ((50, 50, 50, 219, 50, 50), pg.PG_ERR_UNSUPPORTED)])
+def test_bad_bins(eng, bins, code):
+    t = _synth_case(10, 100, 1, seed=1)
+    with pytest.raises(pg.PGError) as e:
+        eng.entropy(t, bins, "hist")
+    assert e.value.code == code
+
+
+def test_context_survives_errors(eng):
+    t = _synth_case(10, 500, 1, seed=1)
+    bad = _synth_case(10, 500, 1, seed=1)
+    bad.bonds[0, 0] = -1.0
+    with pytest.raises(pg.PGError):
+        eng.entropy(bad, (50,) * 6, "hist")
+    body = eng.entropy(t, (50,) * 6, "hist")
+    compare_bodies(7, body, oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6))
+
+
+# ------------------------------------------------------------ size-independent properties
+
+def test_large_properties(eng):
+    """A 900-DOF x 100k-frame FP32 system: every sampled pair's counts sum to F
+    and equal the oracle's; sampled S2D match the oracle's per-pair value; the
+    MI matrix is symmetric; MIST is a spanning tree over all DOFs."""
+    n_atoms, F = 302, 100_000
+    t = _synth_case(n_atoms, F, 0, seed=99, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05)
+    n = n_atoms - 3
+    D = 3 * n + 3
+    body = eng.entropy(t, (50,) * 6, "hist")
+    rng = np.random.default_rng(0)
+    pairs = sorted({tuple(sorted(rng.choice(D, 2, replace=False).tolist())) for _ in range(24)})
+    got = eng.pair_counts(t, (50,) * 6, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, (50,) * 6, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert x.sum() == F and np.array_equal(x, y), p
+    # per-pair S2D against the oracle's direct formula
+    eng.entropy(t, (50,) * 6, "hist", out=body)
+    mn, mx, _, dsh, _ = oracle.extrema(t.bonds, t.angles, t.dihedrals)
+    cols = np.concatenate([t.bonds.astype(np.float64), t.angles.astype(np.float64), dsh])
+    nb, na = n + 2, n + 1
+    typ = lambda g: 0 if g < nb else (1 if g < nb + na else 2)
+    off = {0: 0, 1: nb, 2: nb + na}
+    import ctypes as C
+    for g1, g2 in pairs[:8]:
+        t1, t2 = typ(g1), typ(g2)
+        s_or = oracle.lib().or_entropy2d(t1, oracle._p(np.ascontiguousarray(cols[g1])), mn[g1], mx[g1], 50,
+                                         t2, oracle._p(np.ascontiguousarray(cols[g2])), mn[g2], mx[g2], 50,
+                                         F, None, None)
+        i1, i2 = g1 - off[t1], g2 - off[t2]
+        if t1 == t2:
+            m = (nb, na, n)[t1]
+            idx = (m - i1) * (m - i1 - 1) // 2 + i1 - i2
+            s_gpu = body.blocks[("bb", "aa", "dd")[t1]][idx]
+        else:
+            key = {(0, 1): "ba", (0, 2): "bd", (1, 2): "ad"}[(t1, t2)]
+            s_gpu = body.blocks[key][i1 * (na, n)[t2 - 1] + i2]
+        assert abs(s_gpu - s_or) <= S_TOL, (g1, g2)
+    e, tot = eng.mist(n)
+    assert len(e) == D - 1
+    seen = {(0, 1)}
+    for x in e:
+        assert (x["t1"], x["i1"]) in seen and (x["t2"], x["i2"]) not in seen
+        seen.add((x["t2"], x["i2"]))
+    assert len(seen) == D
