@@ -63,8 +63,9 @@ def parse():
     ap.add_argument("--form", choices=["auto", "hist", "onehot"], default="auto")
     ap.add_argument("--bins", type=int, default=50)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-sample-atoms", type=int, default=16,
-                    help="atoms of the bounded DOF sample timed on the host cores")
+    ap.add_argument("--cpu-sample-atoms", type=int, default=0,
+                    help="atoms of the bounded DOF sample timed on the host cores "
+                         "(0: sized to ~2.5e10 pair-frame updates, about 10 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -130,6 +131,9 @@ def cpu_sample(args, wl):
     import oracle
     import parent_gb300 as pg
     na = args.cpu_sample_atoms
+    if na <= 0:
+        dofs = int((2 * 2.5e10 / F) ** 0.5)
+        na = max(6, min(n_atoms, dofs // 3 + 2))
     t = pg.synth_host(na, F, double_prec=prec, seed=1234, n_latents=lat, frac_bimodal_dih=fbd,
                       frac_bimodal_bond=fbb)
     D = 3 * na - 6
@@ -158,8 +162,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F, "bins": args.bins,
-                   "sample_atoms": args.cpu_sample_atoms},
+        "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F, "bins": args.bins},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

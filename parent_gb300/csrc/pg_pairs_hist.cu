@@ -289,7 +289,7 @@ int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames) {
     for (int T : {4, 2, 1}) {
         for (int fc : fcs) {
             size_t need = T == 4 ? smem_bytes<4>(bmax, fc) : (T == 2 ? smem_bytes<2>(bmax, fc) : smem_bytes<1>(bmax, fc));
-            if (need + 1024 <= (size_t)kSmemMax) {  // static smem of the kernel fits in the rest
+            if (need + 4096 <= (size_t)kSmemMax) {  // the kernel's ~3.3 KB static smem fits in the rest
                 *tile_dim = T;
                 *chunk_frames = fc;
                 return (int)need;

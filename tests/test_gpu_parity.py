@@ -157,6 +157,13 @@ def test_synthetic_matches_oracle(eng, n_atoms, F, prec, bins):
     compare_bodies(n, body, ref)
     e, tot = eng.mist(n)
     re, rt = oracle.mist(n, ref)
+    if np.max(np.abs(re["mi"]), initial=0.0) <= 1e-9:
+        # one 2D bin or one frame: every MI is exactly 0 in exact arithmetic,
+        # so both trees are ordered by ~1e-14 rounding noise; only the values
+        # can agree
+        assert np.max(np.abs(e["mi"]), initial=0.0) <= 1e-9 and np.max(np.abs(re["mi"]), initial=0.0) <= 1e-9
+        assert abs(tot[9] - rt[9]) <= 1e-7
+        return
     compare_mist(e, tot, re, rt)
 
 
