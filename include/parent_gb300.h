@@ -127,6 +127,27 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
 PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mist_edge *edges,
                    double totals[10]);
 
+/* MIST that allocates nothing. It has no counterpart in the reference; it
+ * exists for callers that cannot call cudaMalloc, such as a host program that
+ * owns the whole device memory budget in its own pre-allocated pool, or one
+ * that cannot accept the device-wide synchronisation an allocation or free
+ * may cause while its other streams run.
+ * mi: caller's device buffer, dense symmetric D x D FP64 MI matrix (D =
+ * 3*n_dihedrals+3, global DOF order bonds|angles|dihedrals, diagonal unused);
+ * edge_mi / edge_from / edge_to: caller's device buffers of D-1 entries,
+ * filled with step k's MI, In DOF and Out DOF (global indices), in the order
+ * pg_mist produces them. stream: a cudaStream_t (NULL = default stream); the
+ * call only enqueues, results are ready when the stream reaches them.
+ * D must not exceed PG_NOALLOC_MAX_DOFS (PG_ERR_UNSUPPORTED otherwise). The
+ * per-DOF scratch is one static device array per GPU (16 bytes x
+ * PG_NOALLOC_MAX_DOFS, held until exit) shared by every call: calls that
+ * overlap on the GPU race on it and must be serialised by the caller. The
+ * first call on a device looks up that array's address; make that first call
+ * before any stream capture. */
+#define PG_NOALLOC_MAX_DOFS 16384
+PG_API int pg_mist_noalloc(int n_dihedrals, const double *mi, double *edge_mi, int *edge_from,
+                           int *edge_to, void *stream);
+
 /* Device milliseconds of the kernels of the last pg_entropy / pg_mist call,
  * measured with CUDA events on the context's stream:
  * ms[0] = preprocessing (extrema, modfit, binning, 1D), ms[1] = pair kernel,
