@@ -312,8 +312,8 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     po.counts = nullptr;
     po.counts_bmax = 0;
     if (chosen == PG_FORM_HIST) {
-        int T = 0, fc = 0;
-        if (!pairs_hist_config(bmax_of(g), &T, &fc)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+        int T = 0, fc = 0, nst = 0;
+        if (!pairs_hist_config(bmax_of(g), &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
         if (ctx->tiles_D != g.D || ctx->tiles_T != T) {
             ctx->tiles_host = build_tiles(g.D, T);
             CK(ctx->tiles.ensure(ctx->tiles_host.size() * sizeof(PairTile)));
@@ -382,9 +382,9 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
         if (stride < (int64_t)b1 * b2) return fail(ctx, PG_ERR_ARG, "stride < B1*B2");
     }
     if (n_pairs == 0) return PG_OK;
-    int T = 0, fc = 0;
+    int T = 0, fc = 0, nst = 0;
     const int bm = bmax_of(g);
-    if (!pairs_hist_config(bm, &T, &fc)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+    if (!pairs_hist_config(bm, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
     const int pps = T * T;
     cudaStream_t st = ctx->stream;
     DevBuf tiles;  // private: keep the cached full tile list intact

@@ -96,8 +96,9 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
                               const double *nlogn, const PairTile *tiles, int64_t n_tiles,
                               int tile_dim, PairOut out, int *err, cudaStream_t st);
 // smem bytes the histogram kernel needs for a given max 2D bin count, or 0 if
-// it cannot run; sets *tile_dim (4, 2 or 1 DOFs per tile side).
-int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames);
+// it cannot run; sets *tile_dim (4, 2 or 1 DOFs per tile side) and the
+// staging geometry (frames per chunk, stages).
+int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages);
 
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,

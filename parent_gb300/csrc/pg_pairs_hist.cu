@@ -19,6 +19,7 @@
 // and writes S_ij into the .par body layout and MI into the dense matrix.
 // No histogram ever reaches global memory.
 #include <stdio.h>
+#include <stdlib.h>
 
 #include "pg_internal.h"
 
@@ -26,8 +27,9 @@ namespace pg {
 
 namespace {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
+constexpr int kMaxStages = 4;
 constexpr int kSmemMax = 232448;   // 227 KB opt-in per block on sm_100-class parts
 constexpr int kStagePad = 32;      // bytes between staged rows: puts the 2T rows on distinct banks
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz, then report a timeout
@@ -54,6 +56,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Relaxed arrive: a consumer warp releases a stage after the values it read
+// from it have been used, without waiting for its own shared-memory
+// reductions (which never touch the stage) to drain.
+__device__ __forceinline__ void mbar_arrive_relaxed(uint32_t bar) {
+    asm volatile("mbarrier.arrive.relaxed.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 // Bounded wait: gives up after kWaitCycles and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
     const long long t0 = clock64();
@@ -74,33 +82,34 @@ __host__ __device__ __forceinline__ size_t hist_bytes(int bmax, int pps) {
 }
 
 // hist[word] += 1 in shared memory, result unused
-__device__ __forceinline__ void red_add1(unsigned int *p) {
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(smem_u32(p)) : "memory");
+__device__ __forceinline__ void red_add1_at(uint32_t saddr) {
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr) : "memory");
 }
+__device__ __forceinline__ void red_add1(unsigned int *p) { red_add1_at(smem_u32(p)); }
 
 template <int T>
 struct TileCfg {
     static constexpr int PPS = T * T;      // pair slots
     static constexpr int NSUB = 32 / PPS;  // frame sub-streams per warp
     static constexpr int NROW = 2 * T;     // staged bin rows
+    static constexpr int SHIFT = T == 4 ? 6 : (T == 2 ? 4 : 2);  // log2(PPS * 4)
 };
 
 template <int T>
 __global__ void __launch_bounds__(kThreads, 1)
 pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
                   const double *__restrict__ nlogn, const PairTile *__restrict__ tiles,
-                  PairOut out, int *err, int fc, int bmax, double lnN) {
+                  PairOut out, int *err, int fc, int nst, int bmax, double lnN) {
     using C = TileCfg<T>;
     constexpr int PPS = C::PPS, NSUB = C::NSUB, NROW = C::NROW;
+    constexpr int SH = C::SHIFT;  // log2(bytes between consecutive bins of one slot)
     extern __shared__ __align__(128) unsigned char smem[];
     const int hist_words = bmax * bmax * PPS;
     unsigned int *hist = (unsigned int *)smem;
     const int fcs = fc + kStagePad;
-    unsigned char *stage = smem + hist_bytes(bmax, PPS);  // [2][NROW][fcs], 128-B aligned
-    uint64_t *mbar = (uint64_t *)(stage + 2 * NROW * fcs);
-    __shared__ double red_snl[kWarps][PPS];
-    __shared__ int red_occ[kWarps][PPS];
-    __shared__ int s_abort;
+    unsigned char *stage = smem + hist_bytes(bmax, PPS);  // [nst][NROW][fcs], 128-B aligned
+    uint64_t *mbar = (uint64_t *)(stage + (size_t)nst * NROW * fcs);
+    __shared__ volatile int s_abort;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const PairTile tile = tiles[blockIdx.x];
@@ -112,104 +121,131 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
         return (k - T) < tile.ncol ? tile.col0 + (k - T) : -1;
     };
 
-    for (int i = tid; i < hist_words; i += kThreads) hist[i] = 0u;
+    for (int i = tid * 4; i < hist_words; i += kThreads * 4) {
+        if (i + 4 <= hist_words) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
+        else for (int k = i; k < hist_words; k++) hist[k] = 0u;
+    }
     if (tid == 0) {
         s_abort = 0;
-        mbar_init(smem_u32(&mbar[0]), 1);
-        mbar_init(smem_u32(&mbar[1]), 1);
+        for (int k = 0; k < nst; k++) {
+            mbar_init(smem_u32(&mbar[k]), 1);                            // full[k]: producer + tx bytes
+            mbar_init(smem_u32(&mbar[kMaxStages + k]), kWarps - 1);      // empty[k]: one per consumer warp
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
     const int nchunks = (F + fc - 1) / fc;
-    auto issue = [&](int chunk) {  // one thread
-        const int st = chunk & 1;
-        uint32_t bytes = 0;
-        for (int k = 0; k < NROW; k++) bytes += row_dof(k) >= 0 ? (uint32_t)fc : 0u;
-        const uint32_t bar = smem_u32(&mbar[st]);
-        mbar_expect_tx(bar, bytes);
-        for (int k = 0; k < NROW; k++) {
-            const int g = row_dof(k);
-            if (g < 0) continue;
-            bulk_g2s(smem_u32(stage + (size_t)(st * NROW + k) * fcs),
-                     bins + (int64_t)g * geo.ldb + (int64_t)chunk * fc, (uint32_t)fc, bar);
+    // Warp-specialised pipeline: warp kWarps-1 is the producer (one lane
+    // issues the bulk copies); warps 0..kWarps-2 consume. full[st] completes
+    // when a stage's bytes have landed; empty[st] when every consumer warp is
+    // done reading it. No CTA-wide barrier inside the loop, so the warps'
+    // in-flight shared-memory reductions never have to drain together.
+    constexpr int kConsumers = kWarps - 1;
+    uint64_t *full = mbar, *empty = mbar + kMaxStages;
+    if (warp == kConsumers) {
+        if (lane == 0) {
+            for (int chunk = 0; chunk < nchunks; chunk++) {
+                const int st = chunk % nst;
+                if (chunk >= nst &&
+                    !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((chunk / nst) - 1) & 1))) {
+                    s_abort = 1;
+                    break;
+                }
+                // generic-proxy reads of this stage (released by the empty
+                // barrier) before the async-proxy writes that refill it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                uint32_t bytes = 0;
+                for (int k = 0; k < NROW; k++) bytes += row_dof(k) >= 0 ? (uint32_t)fc : 0u;
+                const uint32_t bar = smem_u32(&full[st]);
+                mbar_expect_tx(bar, bytes);
+                for (int k = 0; k < NROW; k++) {
+                    const int g = row_dof(k);
+                    if (g < 0) continue;
+                    bulk_g2s(smem_u32(stage + (size_t)(st * NROW + k) * fcs),
+                             bins + (int64_t)g * geo.ldb + (int64_t)chunk * fc, (uint32_t)fc, bar);
+                }
+            }
         }
-    };
-    if (tid == 0) {
-        issue(0);
-        if (nchunks > 1) issue(1);
-    }
-
-    // this lane's pair slot
-    const int p = lane % PPS, sub = lane / PPS;
-    const int pr = p / T, pc = p % T;
-    const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
-    const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
-    const bool valid = gr >= 0 && gc >= 0 && gr < gc;
-    const int Bc = valid ? dof.b2[gc] : 0;
-    unsigned int *hp = hist + p;
-
-    for (int chunk = 0; chunk < nchunks; chunk++) {
-        const int st = chunk & 1;
-        const bool ok = mbar_wait_bounded(smem_u32(&mbar[st]), (uint32_t)((chunk >> 1) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) s_abort = 1;
-            break;
-        }
-        const int fvalid = min(fc, F - chunk * fc);
-        const unsigned char *rrow = stage + (size_t)(st * NROW + pr) * fcs;
-        const unsigned char *crow = stage + (size_t)(st * NROW + T + pc) * fcs;
-        if (valid) {
-            for (int off = (warp * NSUB + sub) * 16; off < fvalid; off += kWarps * NSUB * 16) {
-                const uint4 rv = *(const uint4 *)(rrow + off);
-                const uint4 cv = *(const uint4 *)(crow + off);
-                const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
-                const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
-                if (off + 16 <= fvalid) {
+    } else {
+        // this lane's pair slot
+        const int p = lane % PPS, sub = lane / PPS;
+        const int pr = p / T, pc = p % T;
+        const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
+        const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
+        const bool valid = gr >= 0 && gc >= 0 && gr < gc;
+        const uint32_t Bc = valid ? (uint32_t)dof.b2[gc] : 0u;
+        const uint32_t hbase = smem_u32(hist + p);
+        // 16-frame groups go round-robin over the S (warp, sub-stream) slots;
+        // each chunk starts one chunk's group count further along, so the
+        // leftover groups rotate over the warps instead of always landing on
+        // the first ones
+        constexpr int S = kConsumers * NSUB;
+        const int gstep = (fc / 16) % S;
+        int g0 = warp * NSUB + sub;
+        for (int chunk = 0; chunk < nchunks; chunk++) {
+            const int st = chunk % nst;
+            if (!mbar_wait_bounded(smem_u32(&full[st]), (uint32_t)((chunk / nst) & 1))) {
+                s_abort = 1;
+                break;
+            }
+            const int fvalid = min(fc, F - chunk * fc);
+            const unsigned char *rrow = stage + (size_t)(st * NROW + pr) * fcs;
+            const unsigned char *crow = stage + (size_t)(st * NROW + T + pc) * fcs;
+            if (valid) {
+                for (int off = g0 * 16; off < fvalid; off += S * 16) {
+                    const uint4 rv = *(const uint4 *)(rrow + off);
+                    const uint4 cv = *(const uint4 *)(crow + off);
+                    const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                    const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                    if (off + 16 <= fvalid) {
+                        // two frames per 32-bit IMAD: bytes spread into 16-bit
+                        // halves, idx = br*Bc + bc < 65536 never carries across
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-#pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            const uint32_t br = (rw[q] >> (8 * b)) & 0xffu;
-                            const uint32_t bc = (cw[q] >> (8 * b)) & 0xffu;
-                            red_add1(hp + (br * Bc + bc) * PPS);
+                        for (int q = 0; q < 4; q++) {
+                            const uint32_t i01 = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
+                            const uint32_t i23 = __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
+                            red_add1_at(hbase + ((i01 & 0xffffu) << SH));
+                            red_add1_at(hbase + ((i01 >> 16) << SH));
+                            red_add1_at(hbase + ((i23 & 0xffffu) << SH));
+                            red_add1_at(hbase + ((i23 >> 16) << SH));
                         }
-                    }
-                } else {  // ragged end of the trajectory
-                    const int n = fvalid - off;
+                    } else {  // ragged end of the trajectory
+                        const int n = fvalid - off;
 #pragma unroll
-                    for (int k = 0; k < 16; k++) {
-                        if (k < n) {
-                            const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                            const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                            red_add1(hp + (br * Bc + bc) * PPS);
+                        for (int k = 0; k < 16; k++) {
+                            if (k < n) {
+                                const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                red_add1_at(hbase + ((br * Bc + bc) << SH));
+                            }
                         }
                     }
                 }
             }
-        }
-        __syncthreads();
-        if (tid == 0 && chunk + 2 < nchunks) {
-            // generic-proxy reads of this stage are done (barrier above);
-            // order them before the async-proxy writes that refill it
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(chunk + 2);
+            __syncwarp();
+            if (lane == 0) mbar_arrive_relaxed(smem_u32(&empty[st]));
+            g0 -= gstep;
+            if (g0 < 0) g0 += S;
         }
     }
+    __syncthreads();
 
     if (s_abort) {
-        // a stage never completed: record it, drain what is still in flight
-        // (bounded), and leave without writing results
+        // a stage never completed: record it, drain every copy that may still
+        // be in flight (bounded), and leave without writing results
         if (tid == 0) {
             atomicAdd(&err[ERR_TIMEOUT], 1);
-            for (int c = 0; c < nchunks && c < 2; c++) {
-                (void)mbar_wait_bounded(smem_u32(&mbar[c & 1]), 0u);
-            }
+            for (int c = 0; c < nst; c++) (void)mbar_wait_bounded(smem_u32(&full[c]), 0u);
         }
+        __syncthreads();
         return;
     }
 
-    // ---- epilogue: per pair slot, sum n ln n and occupied bins
+    // ---- epilogue: per pair slot, sum n ln n and occupied bins. The staging
+    // area is free now and holds the cross-warp partial sums.
+    double *red_snl = (double *)stage;               // [kWarps][PPS]
+    int *red_occ = (int *)(red_snl + kWarps * PPS);  // [kWarps][PPS]
     const int ep = tid % PPS, ej = tid / PPS;  // kThreads/PPS threads per slot
     const int er = ep / T, ec = ep % T;
     const int egr = er < tile.nrow ? tile.row0 + er : -1;
@@ -237,16 +273,16 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
         occ += __shfl_down_sync(0xffffffffu, occ, o);
     }
     if (lane < PPS) {
-        red_snl[warp][lane] = snl;
-        red_occ[warp][lane] = occ;
+        red_snl[warp * PPS + lane] = snl;
+        red_occ[warp * PPS + lane] = occ;
     }
     __syncthreads();
     if (tid < PPS && evalid) {
         double s = 0.0;
         int o = 0;
         for (int w = 0; w < kWarps; w++) {
-            s += red_snl[w][tid];
-            o += red_occ[w][tid];
+            s += red_snl[w * PPS + tid];
+            o += red_occ[w * PPS + tid];
         }
         const double N = (double)F;
         const double S2 = lnN + dof.acon[egr] + dof.acon[egc] - s / N + (o - 1.0) / (2.0 * N);
@@ -260,8 +296,10 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
 }
 
 template <int T>
-size_t smem_bytes(int bmax, int fc) {
-    return hist_bytes(bmax, TileCfg<T>::PPS) + 2 * TileCfg<T>::NROW * (size_t)(fc + kStagePad) + 16;
+size_t smem_bytes(int bmax, int fc, int nst) {
+    const size_t stage = (size_t)nst * TileCfg<T>::NROW * (fc + kStagePad);
+    const size_t scratch = (size_t)kWarps * TileCfg<T>::PPS * (sizeof(double) + sizeof(int));
+    return hist_bytes(bmax, TileCfg<T>::PPS) + (stage > scratch ? stage : scratch) + 8 * 2 * kMaxStages;
 }
 
 }  // namespace
@@ -284,15 +322,29 @@ __global__ void __launch_bounds__(1024) smem_red_probe(int iters, unsigned int *
     if (threadIdx.x == 0) sink[blockIdx.x] = h[0];
 }
 
-int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames) {
-    const int fcs[3] = {4096, 2048, 1024};
+// Chooses the tile side T (4, 2, 1 DOFs: 16, 4, 1 pair slots) and the
+// staging geometry (frames per chunk x stages) that fit the shared memory for
+// the largest 2D bin count. PG_HIST_FC / PG_HIST_STAGES override the staging
+// for tuning sweeps when they fit.
+int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages) {
+    static const int cand[][2] = {{4096, 2}, {2048, 4}, {2048, 3}, {2048, 2}, {1024, 4}, {1024, 2}};
+    int ofc = 0, onst = 0;
+    if (const char *e = getenv("PG_HIST_FC")) ofc = atoi(e);
+    if (const char *e = getenv("PG_HIST_STAGES")) onst = atoi(e);
     for (int T : {4, 2, 1}) {
-        for (int fc : fcs) {
-            size_t need = T == 4 ? smem_bytes<4>(bmax, fc) : (T == 2 ? smem_bytes<2>(bmax, fc) : smem_bytes<1>(bmax, fc));
-            if (need + 4096 <= (size_t)kSmemMax) {  // the kernel's ~3.3 KB static smem fits in the rest
-                *tile_dim = T;
-                *chunk_frames = fc;
-                return (int)need;
+        auto need = [&](int fc, int nst) -> size_t {
+            return T == 4 ? smem_bytes<4>(bmax, fc, nst)
+                          : (T == 2 ? smem_bytes<2>(bmax, fc, nst) : smem_bytes<1>(bmax, fc, nst));
+        };
+        const bool ovr = ofc >= 512 && ofc <= 8192 && ofc % 512 == 0 && onst >= 2 && onst <= kMaxStages;
+        if (ovr && need(ofc, onst) + 1024 <= (size_t)kSmemMax) {
+            *tile_dim = T; *chunk_frames = ofc; *stages = onst;
+            return (int)need(ofc, onst);
+        }
+        for (const auto &c : cand) {
+            if (need(c[0], c[1]) + 1024 <= (size_t)kSmemMax) {  // + the kernel's static smem
+                *tile_dim = T; *chunk_frames = c[0]; *stages = c[1];
+                return (int)need(c[0], c[1]);
             }
         }
     }
@@ -304,10 +356,11 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
                               int tile_dim, PairOut out, int *err, cudaStream_t st) {
     int bmax = 1;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    int T = 0, fc = 0;
-    const int smem = pairs_hist_config(bmax, &T, &fc);
+    int T = 0, fc = 0, nst = 0;
+    const int smem = pairs_hist_config(bmax, &T, &fc, &nst);
     if (!smem || T != tile_dim) return cudaErrorInvalidValue;
     if (n_tiles <= 0) return cudaSuccess;
+    if ((int64_t)g.ldb < (int64_t)((g.F + fc - 1) / fc) * fc) return cudaErrorInvalidValue;
     const double lnN = log((double)g.F);
     cudaError_t e;
 #define PG_LAUNCH(TT)                                                                              \
@@ -315,7 +368,7 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
                              smem);                                                               \
     if (e != cudaSuccess) return e;                                                               \
     pairs_hist_kernel<TT><<<(unsigned)n_tiles, kThreads, smem, st>>>(g, bins, dof, nlogn, tiles,  \
-                                                                      out, err, fc, bmax, lnN);
+                                                                      out, err, fc, nst, bmax, lnN);
     if (T == 4) { PG_LAUNCH(4) } else if (T == 2) { PG_LAUNCH(2) } else { PG_LAUNCH(1) }
 #undef PG_LAUNCH
     return cudaGetLastError();
