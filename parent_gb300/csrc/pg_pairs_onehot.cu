@@ -1,17 +1,446 @@
-// Pair kernel, tensor-core one-hot form (placeholder until the tcgen05
-// kernel lands) and the form autotuner.
+// Pair kernel, tensor-core one-hot form, and the form autotuner.
+//
+// The 2D histograms of all DOF pairs are the blocks of one Gram matrix
+//   C = X^T X,  X[f, (g, b)] = 1 if DOF g is in bin b at frame f, else 0,
+// whose rows/columns run over the concatenated (DOF, bin) space (R = sum of
+// the DOFs' 2D bin counts). Block (g1, g2) of C is the B(g1) x B(g2)
+// histogram of the pair, so the counts PARENT.cpp fills frame by frame
+// (e.g. :802-804) are entries of C.
+//
+// One CTA computes one 128 x 256 tile of C over all frames with
+// tcgen05.mma.cta_group::1.kind::f8f6f4: A and B are E4M3 one-hot tiles
+// (1.0 = 0x38, 0.0 = 0x00) built in shared memory from the uint8 bin rows,
+// the accumulator is FP32 in tensor memory (256 columns) and exact for counts
+// below 2^24. Eight warps expand 128-frame K-blocks into a 3-stage ring while
+// one elected thread issues the four K=32 MMAs per block and commits them to
+// the stage's mbarrier; a stage is rebuilt only after its MMAs completed.
+//
+// Epilogue: tcgen05.ld brings each row's counts to registers; every count n>0
+// of a pair (g1 < g2) adds round(2^s n ln n) (an int64 table) and 1 to the
+// pair's accumulators. Integer atomics keep the result independent of the
+// order tiles finish in. A finalize kernel turns (sum n ln n, occupied bins)
+// into S2D and MI exactly as the histogram kernel's epilogue does.
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "../../include/parent_gb300.h"
 #include "pg_internal.h"
 
 namespace pg {
 
-bool pairs_onehot_supported(const SysGeom &) { return false; }
-size_t pairs_onehot_scratch_bytes(const SysGeom &) { return 256; }
-cudaError_t launch_pairs_onehot(const SysGeom &, const uint8_t *, const DofArrays &, const double *,
-                                PairOut, int *, cudaStream_t, void *, size_t, int *launches) {
-    *launches = 0;
-    return cudaErrorNotSupported;
+namespace {
+
+constexpr int kThreads = 256;          // 8 warps: builders; warp 0 lane 0 also issues MMAs
+constexpr int kM = 128, kN = 256;      // tile of C
+constexpr int kKB = 128;               // frames per K-block (bytes per row per stage)
+constexpr int kStages = 3;
+constexpr int kAStage = kM * kKB;      // 16 KB
+constexpr int kBStage = kN * kKB;      // 32 KB
+constexpr int kStageBytes = kAStage + kBStage;
+constexpr int kMaxRowDofs = 18, kMaxColDofs = 34;  // 2D bins >= 8
+constexpr long long kWaitCycles = 4000000000LL;
+// Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
+// F ln F * 2^s < 1.6e19, so a pair's sum of n ln n (at most F ln F) fits in
+// an unsigned 64-bit accumulator; the rounding error per occupied bin is
+// 2^-(s+1), i.e. <= 1.2e-13 at 500,000 frames.
+static double fix_scale(int F) {
+    const double top = (double)F * log((double)F > 1 ? (double)F : 2.0) + 1.0;
+    int s = (int)floor(log2(1.6e19 / top));
+    if (s > 44) s = 44;
+    return ldexp(1.0, s);
 }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major: 8-row x 16-byte core
+// matrices stored contiguously (128 B); lbo = byte distance between the two
+// core matrices of one K=32 step, sbo = byte distance between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for sm_100-class tensor cores
+    return d;                // base offset 0, layout type 0 = no swizzle
+}
+
+// Instruction descriptor: D = F32, A = B = E4M3, both K-major, N = 256, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(kM >> 4) << 24);
+
+__device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+struct TcTile {
+    int mt, nt;  // row tile (x128) and column tile (x256) of C
+};
+
+// Per (row, chunk) item of the one-hot build, fixed for the whole K loop.
+struct Item {
+    const uint8_t *src;  // bin row of the item's DOF, frame 0 of its 16-frame chunk
+    uint32_t t4;         // the row's bin replicated in 4 bytes
+    uint32_t dst;        // byte offset inside a stage
+    int c16;             // first frame of the chunk inside a K-block
+    int valid;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
+              const uint32_t *__restrict__ rowinfo,  // (dof << 8) | bin for each row of C
+              const TcTile *__restrict__ tiles, const int64_t *__restrict__ nlogn_fix,
+              unsigned long long *__restrict__ acc_snl, unsigned int *__restrict__ acc_occ, int D,
+              int *err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *stages = smem;  // kStages x (A | B), 1024-B aligned
+    uint64_t *mma_done = (uint64_t *)(smem + kStages * kStageBytes);
+    uint32_t *tmem_slot = (uint32_t *)(mma_done + kStages);
+    unsigned long long *ps_snl = (unsigned long long *)(tmem_slot + 4);  // [kMaxRowDofs][kMaxColDofs]
+    unsigned int *ps_occ = (unsigned int *)(ps_snl + kMaxRowDofs * kMaxColDofs);
+    __shared__ int s_r0dof, s_c0dof;
+    __shared__ int s_cdof[kN];  // DOF of each column of the tile (-1 past R)
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const TcTile tile = tiles[blockIdx.x];
+    const int r0 = tile.mt * kM, c0 = tile.nt * kN;
+
+    if (warp == 0) {  // 256 TMEM columns: the 128 x 256 FP32 accumulator
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(256)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int c = tid; c < kN; c += kThreads) s_cdof[c] = c0 + c < R ? (int)(rowinfo[c0 + c] >> 8) : -1;
+    if (tid == 0) {
+        for (int s = 0; s < kStages; s++) mbar_init(smem_u32(&mma_done[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_r0dof = (int)(rowinfo[r0] >> 8);
+        s_c0dof = (int)(rowinfo[c0 < R ? c0 : R - 1] >> 8);
+    }
+    for (int i = tid; i < kMaxRowDofs * kMaxColDofs; i += kThreads) {
+        ps_snl[i] = 0ull;
+        ps_occ[i] = 0u;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // items: A rows 0..127 (1024 items), then B rows 0..255 (2048 items);
+    // item i -> (row group g, chunk c, row-in-group rr) with rr fastest, so
+    // 8 consecutive threads store one contiguous 128-B core matrix
+    constexpr int kItemsPerThread = (kM + kN) * (kKB / 16) / kThreads;  // 12
+    Item it[kItemsPerThread];
+#pragma unroll
+    for (int j = 0; j < kItemsPerThread; j++) {
+        const int i = tid + j * kThreads;
+        const bool isA = i < kM * 8;
+        const int ii = isA ? i : i - kM * 8;
+        const int rr = ii & 7, c = (ii >> 3) & 7, g = ii >> 6;
+        const int row = (isA ? r0 : c0) + g * 8 + rr;
+        it[j].dst = (isA ? 0u : (uint32_t)kAStage) + (uint32_t)((g * 8 + c) * 128 + rr * 16);
+        it[j].c16 = c * 16;
+        it[j].valid = row < R;
+        const uint32_t info = row < R ? rowinfo[row] : 0u;
+        it[j].src = bins + (int64_t)(info >> 8) * ldb + c * 16;
+        it[j].t4 = (info & 0xffu) * 0x01010101u;
+    }
+
+    const int nkb = (F + kKB - 1) / kKB;
+    const uint32_t sbase = smem_u32(stages);
+    bool aborted = false;  // uniform over the CTA (set from __syncthreads_or)
+    for (int kb = 0; kb < nkb; kb++) {
+        const int s = kb % kStages;
+        if (kb >= kStages) {  // stage s is free once the MMAs of block kb - kStages completed
+            const bool ok = mbar_wait_bounded(smem_u32(&mma_done[s]), (uint32_t)((kb / kStages - 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                aborted = true;
+                break;
+            }
+        }
+        const int fbase = kb * kKB;
+        const int nvalid = F - fbase;  // frames of this block that exist (>= 1)
+        unsigned char *st = stages + s * kStageBytes;
+#pragma unroll
+        for (int j = 0; j < kItemsPerThread; j++) {
+            uint4 o = make_uint4(0u, 0u, 0u, 0u);
+            if (it[j].valid) {
+                const uint4 w = __ldg((const uint4 *)(it[j].src + fbase));
+                o.x = __vcmpeq4(w.x, it[j].t4) & 0x38383838u;
+                o.y = __vcmpeq4(w.y, it[j].t4) & 0x38383838u;
+                o.z = __vcmpeq4(w.z, it[j].t4) & 0x38383838u;
+                o.w = __vcmpeq4(w.w, it[j].t4) & 0x38383838u;
+                if (nvalid < kKB) {  // last block: frames past F are not data
+                    const int v = nvalid - it[j].c16;
+                    uint32_t m[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int bq = v - 4 * q;  // valid bytes in word q
+                        m[q] = bq >= 4 ? 0xffffffffu : (bq <= 0 ? 0u : (0xffffffffu >> (8 * (4 - bq))));
+                    }
+                    o.x &= m[0]; o.y &= m[1]; o.z &= m[2]; o.w &= m[3];
+                }
+            }
+            *(uint4 *)(st + it[j].dst) = o;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core reads
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = sbase + s * kStageBytes, b0 = a0 + kAStage;
+#pragma unroll
+            for (int kk = 0; kk < kKB / 32; kk++) {
+                mma_f8(tmem, smem_desc(a0 + kk * 256, 128, 1024), smem_desc(b0 + kk * 256, 128, 1024),
+                       (kb | kk) != 0);
+            }
+            mma_commit(smem_u32(&mma_done[s]));
+        }
+    }
+
+    // wait for the last MMAs (the commit of the final block covers all earlier ones)
+    if (!aborted && nkb > 0) {
+        const int last = nkb - 1, s = last % kStages;
+        const bool ok = mbar_wait_bounded(smem_u32(&mma_done[s]), (uint32_t)((last / kStages) & 1));
+        if (__syncthreads_or(!ok)) aborted = true;
+    }
+    if (aborted) {
+        if (tid == 0) {
+            atomicAdd(&err[ERR_TIMEOUT], 1);
+            for (int s = 0; s < kStages; s++) (void)mbar_wait_bounded(smem_u32(&mma_done[s]), 0u);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (warp == 0)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+        return;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    // ---- epilogue: warp w reads TMEM lanes 32(w%4).. (tile rows) and
+    // columns (w/4)*128 .. +127
+    const int row = 32 * (warp & 3) + lane;
+    const int grow = r0 + row;
+    const uint32_t rinfo = grow < R ? rowinfo[grow] : 0xffffffffu;
+    const int rdof = grow < R ? (int)(rinfo >> 8) : -1;
+    const int cbase = (warp >> 2) * 128;
+    int cur = -1;
+    unsigned long long snl = 0ull;
+    unsigned int occ = 0u;
+    auto flush = [&](int cdof) {
+        if (cur >= 0 && (snl || occ)) {
+            const int ri = rdof - s_r0dof, ci = cur - s_c0dof;
+            atomicAdd(&ps_snl[ri * kMaxColDofs + ci], snl);
+            atomicAdd(&ps_occ[ri * kMaxColDofs + ci], occ);
+        }
+        cur = cdof;
+        snl = 0ull;
+        occ = 0u;
+    };
+    for (int ch = 0; ch < 8; ch++) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(cbase + ch * 16);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (rdof < 0) continue;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int cdof = s_cdof[cbase + ch * 16 + q];
+            if (cdof < 0) break;        // past the last row of C
+            if (cdof <= rdof) continue;  // only pairs g1 < g2
+            if (cdof != cur) flush(cdof);
+            const unsigned int n = (unsigned int)__float2uint_rn(__uint_as_float(v[q]));
+            if (n) {
+                snl += (unsigned long long)__ldg(nlogn_fix + n);
+                occ++;
+            }
+        }
+    }
+    flush(-1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+    // tile partials -> per-pair accumulators (integer adds: order-independent)
+    for (int i = tid; i < kMaxRowDofs * kMaxColDofs; i += kThreads) {
+        const unsigned int o = ps_occ[i];
+        if (!o) continue;
+        const int g1 = s_r0dof + i / kMaxColDofs, g2 = s_c0dof + i % kMaxColDofs;
+        const int64_t pi = (int64_t)g1 * D + g2;
+        atomicAdd(&acc_snl[pi], ps_snl[i]);
+        atomicAdd(&acc_occ[pi], o);
+    }
+}
+
+// S2D and MI of every pair from the accumulators (the histogram kernel's
+// epilogue formula): S = ln N + A_i + A_j - (1/N) sum n ln n + (occ-1)/(2N).
+__global__ void onehot_finalize(SysGeom geo, DofArrays dof, const unsigned long long *acc_snl,
+                                const unsigned int *acc_occ, PairOut out, double lnN, double fix) {
+    const int D = geo.D;
+    const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g1 = blockIdx.y;
+    if (g2 >= D || g2 <= g1) return;
+    const int64_t pi = (int64_t)g1 * D + g2;
+    const double N = (double)geo.F;
+    const double s = (double)acc_snl[pi] / fix;
+    const unsigned int o = acc_occ[pi];
+    const double S2 = lnN + dof.acon[g1] + dof.acon[g2] - s / N + (o - 1.0) / (2.0 * N);
+    if (out.par) out.par[par_pair_index(out.L, geo.nb, geo.na, geo.nd, g1, g2)] = S2;
+    if (out.mi) {
+        const double mi = dof.s1[g1] + dof.s1[g2] - S2;
+        out.mi[(int64_t)g1 * D + g2] = mi;
+        out.mi[(int64_t)g2 * D + g1] = mi;
+    }
+}
+
+__global__ void nlogn_fix_kernel(int64_t *t, int nmax, double fix) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
+        t[n] = n > 1 ? (int64_t)llrint((double)n * log((double)n) * fix) : 0;
+}
+
+__global__ void rowinfo_kernel(const int *b2, int D, const int64_t *rowstart, uint32_t *rowinfo) {
+    const int g = blockIdx.x;
+    for (int b = threadIdx.x; b < b2[g]; b += blockDim.x) rowinfo[rowstart[g] + b] = ((uint32_t)g << 8) | (uint32_t)b;
+}
+
+size_t smem_bytes() {
+    return (size_t)kStages * kStageBytes + kStages * 8 + 16 +
+           (size_t)kMaxRowDofs * kMaxColDofs * (sizeof(unsigned long long) + sizeof(unsigned int));
+}
+
+}  // namespace
+
+// Host-side geometry of one launch: rows of C, the tile list and the scratch layout.
+struct OnehotPlan {
+    int64_t R = 0, n_tiles = 0;
+    size_t off_rowstart = 0, off_rowinfo = 0, off_tiles = 0, off_fix = 0, off_snl = 0, off_occ = 0, total = 0;
+};
+
+static int bins_of(const SysGeom &g, int gd) { return g.bins[3 + dof_type(gd, g.nb, g.na)]; }
+
+static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles) {
+    OnehotPlan p;
+    std::vector<int64_t> rs((size_t)g.D + 1, 0);
+    for (int d = 0; d < g.D; d++) rs[d + 1] = rs[d] + bins_of(g, d);
+    p.R = rs[g.D];
+    const int64_t mts = (p.R + kM - 1) / kM, nts = (p.R + kN - 1) / kN;
+    auto dof_at = [&](int64_t row) {  // last d with rs[d] <= row
+        return (int)(std::upper_bound(rs.begin(), rs.end(), row) - rs.begin()) - 1;
+    };
+    int64_t cnt = 0;
+    for (int64_t mt = 0; mt < mts; mt++) {
+        const int rdof0 = dof_at(mt * kM);
+        for (int64_t nt = 0; nt < nts; nt++) {
+            const int64_t cend = std::min(p.R, (nt + 1) * kN) - 1;
+            if (dof_at(cend) <= rdof0) continue;  // no pair g1 < g2 in this tile
+            if (tiles) tiles->push_back(TcTile{(int)mt, (int)nt});
+            cnt++;
+        }
+    }
+    p.n_tiles = cnt;
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    p.off_rowstart = 0;
+    p.off_rowinfo = al(p.off_rowstart + sizeof(int64_t) * (g.D + 1));
+    p.off_tiles = al(p.off_rowinfo + sizeof(uint32_t) * (size_t)p.R);
+    p.off_fix = al(p.off_tiles + sizeof(TcTile) * (size_t)cnt);
+    p.off_snl = al(p.off_fix + sizeof(int64_t) * ((size_t)g.F + 1));
+    p.off_occ = al(p.off_snl + sizeof(unsigned long long) * (size_t)g.D * g.D);
+    p.total = al(p.off_occ + sizeof(unsigned int) * (size_t)g.D * g.D);
+    (void)rs;
+    return p;
+}
+
+bool pairs_onehot_supported(const SysGeom &g) {
+    for (int t = 0; t < 3; t++)
+        if (g.bins[3 + t] < 8 || g.bins[3 + t] > 255) return false;  // per-tile DOF tables sized for >= 8 bins
+    return g.F < (1 << 24);  // FP32 accumulators are exact below 2^24
+}
+
+size_t pairs_onehot_scratch_bytes(const SysGeom &g) { return plan(g, nullptr).total; }
+
+cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                                const double *, PairOut out, int *err, cudaStream_t st, void *scratch,
+                                size_t scratch_bytes, int *launches) {
+    *launches = 0;
+    if (!pairs_onehot_supported(g)) return cudaErrorInvalidValue;
+    std::vector<TcTile> tiles;
+    const OnehotPlan p = plan(g, &tiles);
+    if (scratch_bytes < p.total) return cudaErrorInvalidValue;
+    char *base = (char *)scratch;
+    std::vector<int64_t> rs((size_t)g.D + 1, 0);
+    for (int d = 0; d < g.D; d++) rs[d + 1] = rs[d] + bins_of(g, d);
+    int64_t *d_rs = (int64_t *)(base + p.off_rowstart);
+    uint32_t *d_ri = (uint32_t *)(base + p.off_rowinfo);
+    TcTile *d_tiles = (TcTile *)(base + p.off_tiles);
+    int64_t *d_fix = (int64_t *)(base + p.off_fix);
+    unsigned long long *d_snl = (unsigned long long *)(base + p.off_snl);
+    unsigned int *d_occ = (unsigned int *)(base + p.off_occ);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_rs, rs.data(), rs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice, st)))
+        return e;
+    // the host vectors must outlive the copies
+    if ((e = cudaStreamSynchronize(st))) return e;
+    if ((e = cudaMemsetAsync(d_snl, 0, sizeof(unsigned long long) * (size_t)g.D * g.D, st))) return e;
+    if ((e = cudaMemsetAsync(d_occ, 0, sizeof(unsigned int) * (size_t)g.D * g.D, st))) return e;
+    rowinfo_kernel<<<g.D, 64, 0, st>>>(dof.b2, g.D, d_rs, d_ri);
+    const double fix = fix_scale(g.F);
+    nlogn_fix_kernel<<<1024, 256, 0, st>>>(d_fix, g.F, fix);
+    const size_t smem = smem_bytes();
+    if ((e = cudaFuncSetAttribute(onehot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    if (p.n_tiles > 0)
+        onehot_kernel<<<(unsigned)p.n_tiles, kThreads, smem, st>>>(bins, g.ldb, g.F, (int)p.R, d_ri, d_tiles, d_fix,
+                                                                   d_snl, d_occ, g.D, err);
+    dim3 fg((g.D + 255) / 256, g.D);
+    onehot_finalize<<<fg, 256, 0, st>>>(g, dof, d_snl, d_occ, out, log((double)g.F), fix);
+    *launches = 4;
+    return cudaGetLastError();
+}
+
+// Form choice, from the measured GB300 rates at 7,494 DOFs x 500,000 frames:
+// histogram form 3.5 s at 10, 20 and 50 bins (bound by shared-memory
+// reductions, independent of the bin count); one-hot form 11.6 s (10 bins),
+// 39.6 s (20 bins), 208 s (50 bins), bound by its one-hot tile build. The
+// histogram form is faster at every supported bin count, so AUTO picks it;
+// the one-hot form runs when asked for explicitly.
 int autotune_form(const SysGeom &) { return PG_FORM_HIST; }
 
 }  // namespace pg

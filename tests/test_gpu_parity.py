@@ -167,6 +167,40 @@ def test_synthetic_matches_oracle(eng, n_atoms, F, prec, bins):
     compare_mist(e, tot, re, rt)
 
 
+@pytest.mark.parametrize("n_atoms,F,prec,bins", [
+    (100, 20000, 1, (50,) * 6),                      # the CPU-runnable config shape, one-hot form
+    (40, 12345, 0, (10,) * 6),                       # FP32, ragged frame count, 10 bins
+    (30, 5000, 0, (7, 64, 100, 8, 20, 16)),          # different 2D bin counts per type
+    (3, 777, 1, (20,) * 6),                          # no dihedrals
+    (60, 129, 0, (12,) * 6),                         # one K-block plus one frame
+])
+def test_onehot_form_matches_oracle(eng, n_atoms, F, prec, bins):
+    """The tcgen05 one-hot GEMM form: same S2D/MI bars and the same MIST tree."""
+    t = _synth_case(n_atoms, F, prec, seed=n_atoms * 11 + F, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05)
+    body = eng.entropy(t, bins, "onehot")
+    assert eng.last_form() == "onehot"
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    n = n_atoms - 3
+    compare_bodies(n, body, ref)
+    e, tot = eng.mist(n)
+    re, rt = oracle.mist(n, ref)
+    compare_mist(e, tot, re, rt)
+
+
+def test_onehot_and_hist_agree_on_fixture(eng):
+    bat = pg.BatFile(GOLDEN / "ubq_sub.bat")
+    a = eng.entropy(bat.view(), (50,) * 6, "onehot").flat()
+    b = eng.entropy(bat.view(), (50,) * 6, "hist").flat()
+    assert np.max(np.abs(a - b)) <= S_TOL
+
+
+def test_onehot_rejects_tiny_bins(eng):
+    t = _synth_case(10, 300, 1, seed=4)
+    with pytest.raises(pg.PGError) as e:
+        eng.entropy(t, (50, 50, 50, 4, 50, 50), "onehot")
+    assert e.value.code == pg.PG_ERR_UNSUPPORTED
+
+
 def test_counts_bit_exact_mixed_bins(eng):
     t = _synth_case(30, 9000, 0, seed=5, frac_bimodal_dih=0.3)
     bins = (13, 50, 77, 17, 33, 50)
