@@ -7,13 +7,14 @@
 // histogram of the pair, so the counts PARENT.cpp fills frame by frame
 // (e.g. :802-804) are entries of C.
 //
-// One CTA computes one 128 x 256 tile of C over all frames with
-// tcgen05.mma.cta_group::1.kind::f8f6f4: A and B are E4M3 one-hot tiles
-// (1.0 = 0x38, 0.0 = 0x00) built in shared memory from the uint8 bin rows,
-// the accumulator is FP32 in tensor memory (256 columns) and exact for counts
-// below 2^24. Eight warps expand 128-frame K-blocks into a 3-stage ring while
-// one elected thread issues the four K=32 MMAs per block and commits them to
-// the stage's mbarrier; a stage is rebuilt only after its MMAs completed.
+// One CTA computes one 128 x 512 tile of C over all frames with
+// tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256, K=32, two accumulators
+// sharing the A tile): A and B are E4M3 one-hot tiles (1.0 = 0x38, 0.0 = 0x00)
+// built in shared memory from the uint8 bin rows, the accumulators are FP32
+// in tensor memory (all 512 columns) and exact for counts below 2^24. Sixteen
+// warps expand 128-frame K-blocks into a 2-stage ring while one elected thread
+// issues the eight MMAs per block and commits them to the stage's mbarrier; a
+// stage is rebuilt only after its MMAs completed.
 //
 // Epilogue: tcgen05.ld brings each row's counts to registers; every count n>0
 // of a pair (g1 < g2) adds round(2^s n ln n) (an int64 table) and 1 to the
@@ -33,14 +34,24 @@ namespace pg {
 
 namespace {
 
-constexpr int kThreads = 256;          // 8 warps: builders; warp 0 lane 0 also issues MMAs
-constexpr int kM = 128, kN = 256;      // tile of C
+constexpr int kThreads = 512;          // 16 warps: builders; warp 0 lane 0 also issues MMAs
+constexpr int kM = 128, kN = 512;      // tile of C: two 128 x 256 accumulators share one A tile
+constexpr int kNH = 256;               // N of one MMA
 constexpr int kKB = 128;               // frames per K-block (bytes per row per stage)
-constexpr int kStages = 3;
+constexpr int kStages = 2;
 constexpr int kAStage = kM * kKB;      // 16 KB
-constexpr int kBStage = kN * kKB;      // 32 KB
+constexpr int kBStage = kN * kKB;      // 64 KB
 constexpr int kStageBytes = kAStage + kBStage;
-constexpr int kMaxRowDofs = 18, kMaxColDofs = 34;  // 2D bins >= 8
+constexpr int kMaxRowDofs = 18, kMaxColDofs = 66;  // 2D bins >= 8
+constexpr int kBinSlots = kMaxRowDofs + kMaxColDofs;
+constexpr int kBinBufBytes = kBinSlots * kKB;      // one K-block of the tile's bin rows
+// byte offsets inside the dynamic shared memory
+constexpr int kOffBar = kStages * kStageBytes;
+constexpr int kOffTmem = kOffBar + kStages * 8;
+constexpr int kOffPsSnl = (kOffTmem + 16 + 15) / 16 * 16;
+constexpr int kOffPsOcc = kOffPsSnl + kMaxRowDofs * kMaxColDofs * 8;
+constexpr int kOffBins = (kOffPsOcc + kMaxRowDofs * kMaxColDofs * 4 + 127) / 128 * 128;
+constexpr int kSmemBytes = kOffBins + 2 * kBinBufBytes;
 constexpr long long kWaitCycles = 4000000000LL;
 // Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
 // F ln F * 2^s < 1.6e19, so a pair's sum of n ln n (at most F ln F) fits in
@@ -91,8 +102,19 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 }
 
 // Instruction descriptor: D = F32, A = B = E4M3, both K-major, N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kN >> 3) << 17) |
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kNH >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
+
+// E4M3 one-hot of 4 bins against a bin replicated in t4: 0x38 (1.0) in every
+// byte where w equals t4, 0x00 elsewhere. x = w ^ t4 has a zero byte exactly
+// where they match; adding 0x7F to the low 7 bits of each byte sets bit 7 of
+// every byte that is nonzero without carrying into its neighbour, so the
+// complement of (sum | x | 0x7F7F7F7F) keeps bit 7 of the zero bytes only.
+__device__ __forceinline__ uint32_t onehot4(uint32_t w, uint32_t t4) {
+    const uint32_t x = w ^ t4;
+    const uint32_t y = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+    return (y >> 7) * 0x38u;
+}
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
     asm volatile(
@@ -107,13 +129,15 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
+__device__ __forceinline__ unsigned char *bin_buffer(unsigned char *smem) { return smem + kOffBins; }
+
 struct TcTile {
-    int mt, nt;  // row tile (x128) and column tile (x256) of C
+    int mt, nt;  // row tile (x128) and column tile (x512) of C
 };
 
 // Per (row, chunk) item of the one-hot build, fixed for the whole K loop.
 struct Item {
-    const uint8_t *src;  // bin row of the item's DOF, frame 0 of its 16-frame chunk
+    uint32_t soff;       // offset of the item's 16 bin bytes inside a bin buffer
     uint32_t t4;         // the row's bin replicated in 4 bytes
     uint32_t dst;        // byte offset inside a stage
     int c16;             // first frame of the chunk inside a K-block
@@ -128,10 +152,10 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
               int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *stages = smem;  // kStages x (A | B), 1024-B aligned
-    uint64_t *mma_done = (uint64_t *)(smem + kStages * kStageBytes);
-    uint32_t *tmem_slot = (uint32_t *)(mma_done + kStages);
-    unsigned long long *ps_snl = (unsigned long long *)(tmem_slot + 4);  // [kMaxRowDofs][kMaxColDofs]
-    unsigned int *ps_occ = (unsigned int *)(ps_snl + kMaxRowDofs * kMaxColDofs);
+    uint64_t *mma_done = (uint64_t *)(smem + kOffBar);
+    uint32_t *tmem_slot = (uint32_t *)(smem + kOffTmem);
+    unsigned long long *ps_snl = (unsigned long long *)(smem + kOffPsSnl);  // [kMaxRowDofs][kMaxColDofs]
+    unsigned int *ps_occ = (unsigned int *)(smem + kOffPsOcc);
     __shared__ int s_r0dof, s_c0dof;
     __shared__ int s_cdof[kN];  // DOF of each column of the tile (-1 past R)
 
@@ -139,9 +163,9 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     const TcTile tile = tiles[blockIdx.x];
     const int r0 = tile.mt * kM, c0 = tile.nt * kN;
 
-    if (warp == 0) {  // 256 TMEM columns: the 128 x 256 FP32 accumulator
+    if (warp == 0) {  // all 512 TMEM columns: two 128 x 256 FP32 accumulators
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(256)
+                     "r"(512)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -160,11 +184,30 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    const int rdof0 = s_r0dof, cdof0 = s_c0dof;
+    const int rlast = (int)(rowinfo[min(r0 + kM, R) - 1] >> 8);
+    const int clast = (int)(rowinfo[min(c0 + kN, R) - 1] >> 8);
 
-    // items: A rows 0..127 (1024 items), then B rows 0..255 (2048 items);
+    // Shared double buffer of the tile's bin rows for one K-block,
+    // [2][kBinSlots][kKB]: slot k < kMaxRowDofs holds DOF rdof0 + k (rows of
+    // A), slot kMaxRowDofs + k holds DOF cdof0 + k (rows of B). Each K-block
+    // the CTA loads the next block's 16-byte chunks into registers first and
+    // stores them after building the current block, so the loads' latency
+    // hides behind the build.
+    unsigned char *binbuf = bin_buffer(smem);
+    constexpr int kLoads = kBinSlots * (kKB / 16);  // 16-byte chunks per K-block
+    auto load_chunk = [&](int L, int fbase, uint4 &v) -> bool {
+        const int slot = L >> 3, c = L & 7;
+        const int d = slot < kMaxRowDofs ? rdof0 + slot : cdof0 + slot - kMaxRowDofs;
+        const bool ok = slot < kMaxRowDofs ? d <= rlast : d <= clast;
+        if (ok) v = __ldg((const uint4 *)(bins + (int64_t)d * ldb + fbase + c * 16));
+        return ok;
+    };
+
+    // items: A rows 0..127 (1024 items), then B rows 0..511 (4096 items);
     // item i -> (row group g, chunk c, row-in-group rr) with rr fastest, so
     // 8 consecutive threads store one contiguous 128-B core matrix
-    constexpr int kItemsPerThread = (kM + kN) * (kKB / 16) / kThreads;  // 12
+    constexpr int kItemsPerThread = (kM + kN) * (kKB / 16) / kThreads;  // 10
     Item it[kItemsPerThread];
 #pragma unroll
     for (int j = 0; j < kItemsPerThread; j++) {
@@ -177,12 +220,21 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
         it[j].c16 = c * 16;
         it[j].valid = row < R;
         const uint32_t info = row < R ? rowinfo[row] : 0u;
-        it[j].src = bins + (int64_t)(info >> 8) * ldb + c * 16;
+        const int d = (int)(info >> 8);
+        const int slot = isA ? d - rdof0 : kMaxRowDofs + d - cdof0;
+        it[j].soff = row < R ? (uint32_t)(slot * kKB + c * 16) : 0u;
         it[j].t4 = (info & 0xffu) * 0x01010101u;
     }
 
     const int nkb = (F + kKB - 1) / kKB;
     const uint32_t sbase = smem_u32(stages);
+    // K-block 0's bin rows into buffer 0
+    for (int L = tid; L < kLoads; L += kThreads) {
+        uint4 v;
+        if (load_chunk(L, 0, v)) *(uint4 *)(binbuf + (L >> 3) * kKB + (L & 7) * 16) = v;
+    }
+    __syncthreads();
+
     bool aborted = false;  // uniform over the CTA (set from __syncthreads_or)
     for (int kb = 0; kb < nkb; kb++) {
         const int s = kb % kStages;
@@ -195,16 +247,27 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
         }
         const int fbase = kb * kKB;
         const int nvalid = F - fbase;  // frames of this block that exist (>= 1)
+        // prefetch the next block's bin rows into registers
+        uint4 pf[2];
+        bool pv[2] = {false, false};
+        if (kb + 1 < nkb) {
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int L = tid + q * kThreads;
+                if (L < kLoads) pv[q] = load_chunk(L, fbase + kKB, pf[q]);
+            }
+        }
+        const unsigned char *bb = binbuf + (kb & 1) * kBinBufBytes;
         unsigned char *st = stages + s * kStageBytes;
 #pragma unroll
         for (int j = 0; j < kItemsPerThread; j++) {
             uint4 o = make_uint4(0u, 0u, 0u, 0u);
             if (it[j].valid) {
-                const uint4 w = __ldg((const uint4 *)(it[j].src + fbase));
-                o.x = __vcmpeq4(w.x, it[j].t4) & 0x38383838u;
-                o.y = __vcmpeq4(w.y, it[j].t4) & 0x38383838u;
-                o.z = __vcmpeq4(w.z, it[j].t4) & 0x38383838u;
-                o.w = __vcmpeq4(w.w, it[j].t4) & 0x38383838u;
+                const uint4 w = *(const uint4 *)(bb + it[j].soff);
+                o.x = onehot4(w.x, it[j].t4);
+                o.y = onehot4(w.y, it[j].t4);
+                o.z = onehot4(w.z, it[j].t4);
+                o.w = onehot4(w.w, it[j].t4);
                 if (nvalid < kKB) {  // last block: frames past F are not data
                     const int v = nvalid - it[j].c16;
                     uint32_t m[4];
@@ -218,6 +281,13 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             }
             *(uint4 *)(st + it[j].dst) = o;
         }
+        // the other buffer was last read while building block kb-1 (before the
+        // previous barrier): it can take the prefetched rows now
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int L = tid + q * kThreads;
+            if (pv[q]) *(uint4 *)(binbuf + ((kb + 1) & 1) * kBinBufBytes + (L >> 3) * kKB + (L & 7) * 16) = pf[q];
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core reads
         __syncthreads();
         if (tid == 0) {
@@ -225,8 +295,11 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             const uint32_t a0 = sbase + s * kStageBytes, b0 = a0 + kAStage;
 #pragma unroll
             for (int kk = 0; kk < kKB / 32; kk++) {
-                mma_f8(tmem, smem_desc(a0 + kk * 256, 128, 1024), smem_desc(b0 + kk * 256, 128, 1024),
-                       (kb | kk) != 0);
+#pragma unroll
+                for (int h = 0; h < kN / kNH; h++) {  // B rows h*256.. start 32 row groups (32 KB) further
+                    mma_f8(tmem + h * kNH, smem_desc(a0 + kk * 256, 128, 1024),
+                           smem_desc(b0 + h * (kNH / 8) * 1024 + kk * 256, 128, 1024), (kb | kk) != 0);
+                }
             }
             mma_commit(smem_u32(&mma_done[s]));
         }
@@ -246,13 +319,13 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         if (warp == 0)
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
         return;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     // ---- epilogue: warp w reads TMEM lanes 32(w%4).. (tile rows) and
-    // columns (w/4)*128 .. +127
+    // columns (w/4)*128 .. +127 (16 warps cover the 512 columns)
     const int row = 32 * (warp & 3) + lane;
     const int grow = r0 + row;
     const uint32_t rinfo = grow < R ? rowinfo[grow] : 0xffffffffu;
@@ -298,7 +371,7 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
     // tile partials -> per-pair accumulators (integer adds: order-independent)
     for (int i = tid; i < kMaxRowDofs * kMaxColDofs; i += kThreads) {
         const unsigned int o = ps_occ[i];
@@ -341,10 +414,7 @@ __global__ void rowinfo_kernel(const int *b2, int D, const int64_t *rowstart, ui
     for (int b = threadIdx.x; b < b2[g]; b += blockDim.x) rowinfo[rowstart[g] + b] = ((uint32_t)g << 8) | (uint32_t)b;
 }
 
-size_t smem_bytes() {
-    return (size_t)kStages * kStageBytes + kStages * 8 + 16 +
-           (size_t)kMaxRowDofs * kMaxColDofs * (sizeof(unsigned long long) + sizeof(unsigned int));
-}
+size_t smem_bytes() { return (size_t)kSmemBytes; }
 
 }  // namespace
 
@@ -435,12 +505,16 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
     return cudaGetLastError();
 }
 
-// Form choice, from the measured GB300 rates at 7,494 DOFs x 500,000 frames:
-// histogram form 3.5 s at 10, 20 and 50 bins (bound by shared-memory
-// reductions, independent of the bin count); one-hot form 11.6 s (10 bins),
-// 39.6 s (20 bins), 208 s (50 bins), bound by its one-hot tile build. The
-// histogram form is faster at every supported bin count, so AUTO picks it;
-// the one-hot form runs when asked for explicitly.
-int autotune_form(const SysGeom &) { return PG_FORM_HIST; }
+// Form choice, from measured GB300 pair-kernel times at 7,494 DOFs x 500,000
+// frames: the histogram form takes ~3.5 s at any bin count (bound by
+// shared-memory reductions, one per update); the one-hot form takes 2.1 s at
+// 10 bins, 8.1 s at 20 and 50 s at 50 (B1*B2 FP8 MACs per update, bound by
+// its one-hot tile build). Its time grows as B^2, so it wins up to ~12 bins.
+int autotune_form(const SysGeom &g) {
+    int bmax = 0;
+    for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
+    if (pairs_onehot_supported(g) && bmax <= 12 && g.F >= 4096) return PG_FORM_ONEHOT;
+    return PG_FORM_HIST;
+}
 
 }  // namespace pg
