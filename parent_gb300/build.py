@@ -35,6 +35,7 @@ CU_SOURCES = {
     "pg_api.cu": [],
     "pg_prep.cu": ["--fmad=false"],
     "pg_pairs_hist.cu": [],
+    "pg_pairs_hist32.cu": [],
     "pg_pairs_onehot.cu": [],
     "pg_mist.cu": [],
     "pg_synth.cu": [],

@@ -240,6 +240,57 @@ static int bmax_of(const SysGeom &g) {
     return std::max(g.bins[3], std::max(g.bins[4], g.bins[5]));
 }
 
+// Histogram layout: the 16-slot kernel (32-bit counters, two frame
+// sub-streams per pair) is the default; it measured 3.47 s against 5.40 s for
+// the 32-slot kernel (16-bit conflict-free counters with windowed folding) at
+// 7,494 DOFs x 500,000 frames x 50 bins. PG_HIST_SLOTS=32 selects the latter
+// (2D bins <= 50).
+static bool use_hist32(const SysGeom &g) {
+    const char *e = getenv("PG_HIST_SLOTS");
+    return e && atoi(e) == 32 && pairs_hist32_supported(bmax_of(g));
+}
+
+// Launches the 32-slot kernel over the cached full tile list (explicit ==
+// nullptr) or over n_explicit given tiles; the per-CTA accumulators live in
+// ctx->scratch.
+static int run_hist32(pg_ctx *ctx, const SysGeom &g, const DofArrays &dof, const PairOut &po,
+                      const PairTile *explicit_tiles, int64_t n_explicit) {
+    cudaStream_t st = ctx->stream;
+    const PairTile *tiles;
+    int64_t n;
+    DevBuf ex;
+    if (explicit_tiles) {
+        CK(ex.ensure(sizeof(PairTile) * (size_t)std::max<int64_t>(n_explicit, 1)));
+        CK(cudaMemcpyAsync(ex.p, explicit_tiles, sizeof(PairTile) * n_explicit, cudaMemcpyHostToDevice, st));
+        tiles = (const PairTile *)ex.p;
+        n = n_explicit;
+    } else {
+        if (ctx->tiles_D != g.D || ctx->tiles_T != 32) {
+            ctx->tiles_host = build_tiles32(g.D);
+            CK(ctx->tiles.ensure(ctx->tiles_host.size() * sizeof(PairTile)));
+            CK(cudaMemcpyAsync(ctx->tiles.p, ctx->tiles_host.data(), ctx->tiles_host.size() * sizeof(PairTile),
+                               cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
+            ctx->tiles_D = g.D;
+            ctx->tiles_T = 32;
+        }
+        tiles = (const PairTile *)ctx->tiles.p;
+        n = (int64_t)ctx->tiles_host.size();
+    }
+    int n_sm = 0;
+    CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(n, n_sm));
+    const size_t sb = pairs_hist32_scratch_bytes(bmax_of(g), grid);
+    CK(ctx->scratch.ensure(sb));
+    CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const double *)ctx->nlogn.p, tiles, n, grid, po,
+                           (int *)ctx->errw.p, ctx->scratch.p, sb, st));
+    ctx->launches++;
+    if (explicit_tiles) {
+        CK(cudaStreamSynchronize(st));  // the private tile buffer is released on return
+    }
+    return PG_OK;
+}
+
 extern "C" {
 
 PG_API const char *pg_last_global_error(void) { return g_global_err.c_str(); }
@@ -311,7 +362,10 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     po.L = L;
     po.counts = nullptr;
     po.counts_bmax = 0;
-    if (chosen == PG_FORM_HIST) {
+    if (chosen == PG_FORM_HIST && use_hist32(g)) {
+        int rc2 = run_hist32(ctx, g, dof, po, nullptr, 0);
+        if (rc2) return rc2;
+    } else if (chosen == PG_FORM_HIST) {
         int T = 0, fc = 0, nst = 0;
         if (!pairs_hist_config(bmax_of(g), &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
         if (ctx->tiles_D != g.D || ctx->tiles_T != T) {
@@ -382,25 +436,34 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
         if (stride < (int64_t)b1 * b2) return fail(ctx, PG_ERR_ARG, "stride < B1*B2");
     }
     if (n_pairs == 0) return PG_OK;
-    int T = 0, fc = 0, nst = 0;
     const int bm = bmax_of(g);
-    if (!pairs_hist_config(bm, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
-    const int pps = T * T;
     cudaStream_t st = ctx->stream;
-    DevBuf tiles;  // private: keep the cached full tile list intact
-    CK(tiles.ensure(t.size() * sizeof(PairTile)));
-    CK(ctx->counts.ensure((size_t)n_pairs * pps * bm * bm * sizeof(int64_t)));
-    CK(cudaMemcpyAsync(tiles.p, t.data(), t.size() * sizeof(PairTile), cudaMemcpyHostToDevice, st));
     PairOut po;
     po.par = nullptr;
     po.mi = nullptr;
     po.L = par_layout(g.n_dih);
-    po.counts = (int64_t *)ctx->counts.p;
     po.counts_bmax = bm;
-    cudaError_t e = launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof_arrays(ctx, g.D),
-                                      (const double *)ctx->nlogn.p, (const PairTile *)tiles.p, n_pairs, T,
-                                      po, (int *)ctx->errw.p, st);
-    ctx->launches++;
+    int pps;
+    cudaError_t e = cudaSuccess;
+    DevBuf tiles;  // private: keep the cached full tile list intact
+    if (use_hist32(g)) {
+        pps = 32;
+        CK(ctx->counts.ensure((size_t)n_pairs * pps * bm * bm * sizeof(int64_t)));
+        po.counts = (int64_t *)ctx->counts.p;
+        int rc2 = run_hist32(ctx, g, dof_arrays(ctx, g.D), po, t.data(), n_pairs);
+        if (rc2) return rc2;
+    } else {
+        int T = 0, fc = 0, nst = 0;
+        if (!pairs_hist_config(bm, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+        pps = T * T;
+        CK(tiles.ensure(t.size() * sizeof(PairTile)));
+        CK(ctx->counts.ensure((size_t)n_pairs * pps * bm * bm * sizeof(int64_t)));
+        CK(cudaMemcpyAsync(tiles.p, t.data(), t.size() * sizeof(PairTile), cudaMemcpyHostToDevice, st));
+        po.counts = (int64_t *)ctx->counts.p;
+        e = launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof_arrays(ctx, g.D), (const double *)ctx->nlogn.p,
+                              (const PairTile *)tiles.p, n_pairs, T, po, (int *)ctx->errw.p, st);
+        ctx->launches++;
+    }
     if (e == cudaSuccess) {
         for (int k = 0; k < n_pairs && e == cudaSuccess; k++) {
             const int b1 = g.bins[3 + dof_type(g1[k], g.nb, g.na)], b2 = g.bins[3 + dof_type(g2[k], g.nb, g.na)];

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace pg {
 
 // DOF type codes (reference util.h:33-35).
@@ -100,6 +102,15 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
 // staging geometry (frames per chunk, stages).
 int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages);
 
+// 32-slot histogram pair kernel (2D bins <= 50): 16-bit conflict-free
+// counters folded into a per-CTA 32-bit accumulator (scratch) every 63,488
+// frames; persistent grid of `grid` CTAs over 4 x 8-DOF tiles.
+bool pairs_hist32_supported(int bmax);
+size_t pairs_hist32_scratch_bytes(int bmax, int grid);
+cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, const double *nlogn,
+                                const PairTile *tiles, int64_t n_tiles, int grid, PairOut out, int *err,
+                                void *scratch, size_t scratch_bytes, cudaStream_t st);
+
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const double *nlogn, PairOut out, int *err, cudaStream_t st,
@@ -110,5 +121,7 @@ bool pairs_onehot_supported(const SysGeom &g);
 // MI matrix from a .par body already on the device (get_mutual semantics).
 cudaError_t launch_mi_from_par(int n_dih, const double *par, ParLayout L, double *mi,
                                cudaStream_t st);
+
+std::vector<PairTile> build_tiles32(int D);
 
 }  // namespace pg

@@ -83,7 +83,7 @@ __host__ __device__ __forceinline__ size_t hist_bytes(int bmax, int pps) {
 
 // hist[word] += 1 in shared memory, result unused
 __device__ __forceinline__ void red_add1_at(uint32_t saddr) {
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr) : "memory");
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr));  // ordering comes from the arrive/barrier clobbers
 }
 __device__ __forceinline__ void red_add1(unsigned int *p) { red_add1_at(smem_u32(p)); }
 

@@ -327,3 +327,20 @@ def test_large_properties(eng):
         assert (x["t1"], x["i1"]) in seen and (x["t2"], x["i2"]) not in seen
         seen.add((x["t2"], x["i2"]))
     assert len(seen) == D
+
+
+@pytest.mark.parametrize("n_atoms,F,bins", [(40, 70000, (50,) * 6), (20, 3000, (10, 20, 30, 50, 20, 8))])
+def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
+    """The 32-slot histogram layout (16-bit counters folded into 32-bit every
+    63,488 frames; F = 70,000 crosses one fold) gives the same counts and values."""
+    monkeypatch.setenv("PG_HIST_SLOTS", "32")
+    t = _synth_case(n_atoms, F, 0, seed=n_atoms + F, frac_bimodal_dih=0.2)
+    body = eng.entropy(t, bins, "hist")
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    compare_bodies(n_atoms - 3, body, ref)
+    D = 3 * n_atoms - 6
+    pairs = [(0, 1), (0, D - 1), (5, 17), (D - 2, D - 1)]
+    got = eng.pair_counts(t, bins, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, bins, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
