@@ -48,6 +48,9 @@ WORKLOADS = {
     "stress_14994dof_1m": (5000, 1_000_000, 0, 0.0, 0.0, 8),
     "small_600dof_50k": (203, 50_000, 0, 0.2, 0.05, 8),
 }
+# 64 independent systems: atoms ~ U[50,800], frames log-uniform in
+# [5,000, 100,000], FP32, latents ~ U[2,16], one seed per system
+BATCH = "batch64_50to800atoms_5k100kframes"
 DEFAULT = "protein_dimer_7494dof_500k"
 METRIC = "DOF-pair x frame updates/s @50 bins (all-pairs 2D-histogram MI + MIST)"
 UNIT = "updates/s"
@@ -59,7 +62,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + [BATCH], default=DEFAULT)
     ap.add_argument("--form", choices=["auto", "hist", "onehot"], default="auto")
     ap.add_argument("--bins", type=int, default=50)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -147,7 +150,9 @@ def cpu_sample(args, wl):
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
-    wl = WORKLOADS[args.workload]
+    # the batch workload is sampled as one system of its largest atom count at
+    # its mean frame count
+    wl = WORKLOADS[args.workload] if args.workload in WORKLOADS else (800, 31_700, 0, 0.0, 0.0, 8)
     if rank != 0:
         return 0
     vals = []
@@ -172,7 +177,181 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU leg
 
+def batch_systems(seed: int = 64, n: int = 64):
+    """(n_atoms, frames, latents, seed) of the batch workload's systems."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        atoms = int(rng.integers(50, 801))
+        frames = int(round(float(np.exp(rng.uniform(np.log(5000.0), np.log(100000.0))))))
+        lat = int(rng.integers(2, 17))
+        out.append((atoms, frames, lat, 1000 + 17 * k))
+    return out
+
+
+def run_batch(args):
+    """The batch workload: pg_entropy_batch (one pair launch over every
+    system's tiles + one MIST launch, replayed from a captured CUDA graph)
+    against the same 64 systems run one after another through pg_entropy +
+    pg_mist. value = batched updates/s; the sequential figure is reported
+    beside it."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    import parent_gb300 as pg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    bins = (args.bins,) * 6
+    systems = batch_systems(seed=64 + rank)
+    es = 4
+    eng = pg.Engine(local)
+    sizes = [(3 * a - 6) * f * es for a, f, _, _ in systems]
+    total_bytes = sum(sizes)
+    dbuf = eng.alloc(total_bytes)
+    views, units = [], 0
+    off = 0
+    for (a, f, lat, sd), nbytes in zip(systems, sizes):
+        nd = a - 3
+        nb, na = nd + 2, nd + 1
+        p = dbuf + off
+        ptrs = (p, p + nb * f * es, p + (nb + na) * f * es)
+        eng.synth_device(a, f, 0, ptrs, f, seed=sd + 7919 * rank, n_latents=lat, frac_bimodal_dih=0.0,
+                         frac_bimodal_bond=0.0)
+        views.append(pg.BatView(nd, f, 0, 1, f, *ptrs))
+        D = 3 * a - 6
+        units += D * (D - 1) // 2 * f
+        off += nbytes
+    stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
+
+    def batched():
+        eng.entropy_batch(views, bins, args.form, bodies=False, trees=True)
+
+    def sequential():
+        for v in views:
+            eng.entropy(v, bins, args.form, keep_result=False)
+            eng.mist(v.n_dihedrals)
+
+    def timed(fn, steps):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(local)
+        eng.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            fn()
+        ev1.record(stream)
+        ev1.synchronize()
+        eng.synchronize()
+        torch.cuda.synchronize(local)
+        ms = ev0.elapsed_time(ev1)
+        if dist:
+            tt = torch.tensor([ms], device=f"cuda:{local}")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms / steps
+
+    for _ in range(args.warmup):
+        batched()
+    launches0 = eng.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_batch = timed(batched, args.steps)
+    clk = clocks.stop()
+    launches = eng.launch_count() - launches0
+    graph_ms = float(eng.timings()[1])
+    sequential()
+    ms_seq = timed(sequential, max(1, min(args.steps, 2)))
+    value = units * world / (ms_batch / 1e3)
+
+    e2e = None
+    if args.e2e_steps > 0:
+        host = C.c_void_p()
+        pg._check(pg.lib().pg_host_alloc_pinned(total_bytes, C.byref(host)))
+        eng.memcpy(host.value, dbuf, total_bytes, 2)
+        eng.synchronize()
+        hviews, off = [], 0
+        for v, nbytes in zip(views, sizes):
+            nd, f = v.n_dihedrals, v.n_frames
+            p = host.value + off
+            hviews.append(pg.BatView(nd, f, 0, 0, f, p, p + (nd + 2) * f * es, p + (2 * nd + 3) * f * es))
+            off += nbytes
+        body_elems = [sum(pg.block_sizes(v.n_dihedrals).values()) for v in views]
+        hout = C.c_void_p()
+        pg._check(pg.lib().pg_host_alloc_pinned(sum(body_elems) * 8, C.byref(hout)))
+        flat = np.ctypeslib.as_array(C.cast(hout, C.POINTER(C.c_double)), (sum(body_elems),))
+        bodies, o = [], 0
+        for v in views:
+            blocks = {}
+            for k, n in pg.block_sizes(v.n_dihedrals).items():
+                blocks[k] = flat[o:o + n]
+                o += n
+            bodies.append(pg.ParBody(v.n_dihedrals, blocks))
+        eng.entropy_batch(hviews, bins, args.form, bodies=bodies, trees=True)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            eng.entropy_batch(hviews, bins, args.form, bodies=bodies, trees=True)
+        sec = (time.perf_counter() - t0) / args.e2e_steps
+        if dist:
+            tt = torch.tensor([sec], device=f"cuda:{local}")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            sec = float(tt.item())
+        n_edges = sum(3 * v.n_dihedrals + 2 for v in views)
+        e2e = {"value": units * world / sec, "unit": UNIT, "h2d_bytes_per_step": total_bytes,
+               "d2h_bytes_per_step": sum(body_elems) * 8 + n_edges * 32 + 80 * len(views),
+               "ms_per_step": sec * 1e3}
+        pg._check(pg.lib().pg_host_free_pinned(host))
+        pg._check(pg.lib().pg_host_free_pinned(hout))
+
+    red_peak = eng.probe_smem_red_rate()
+    achieved = units / (graph_ms / 1e3)
+    roofline = {"bound": "smem", "achieved": achieved / 1e9, "peak": red_peak / 1e9, "unit": "Gred/s",
+                "frac": achieved / red_peak, "traffic": None,
+                "note": "whole captured graph (64 preps + one pair launch + one MIST launch) timed; one "
+                        "shared-memory reduction per update; peak = live conflict-free red.shared rate"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, sample, threads, _ = cpu_sample(args, (800, 31_700, 0, 0.0, 0.0, 8))
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": sample + " (one system of the batch's largest atom count at its mean frame count)"}
+    if rank == 0:
+        Ds = [3 * a - 6 for a, _, _, _ in systems]
+        Fs = [f for _, f, _, _ in systems]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": BATCH, "systems": len(systems), "dofs": [min(Ds), max(Ds)],
+                       "frames": [min(Fs), max(Fs)], "updates_per_step": units, "input": "fp32",
+                       "bins": args.bins, "form": "hist",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
+                       "l2": "inputs (%.1f GB) larger than L2; no flush" % (total_bytes / 1e9)},
+            "sequential": {"ms_per_step": ms_seq, "value": units * world / (ms_seq / 1e3),
+                           "speedup_of_batch": ms_seq / ms_batch},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    eng.free(dbuf)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_gb300(args):
+    if args.workload == BATCH:
+        return run_batch(args)
     import torch
     import parent_gb300 as pg
 

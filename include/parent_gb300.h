@@ -148,6 +148,17 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
 PG_API int pg_mist_noalloc(int n_dihedrals, const double *mi, double *edge_mi, int *edge_from,
                            int *edge_to, void *stream);
 
+/* Many independent trajectories in one run (no reference counterpart: the
+ * reference handles one trajectory per PARENT.x / get_PAR_MIST.x process).
+ * Every system gets the PARENT.x computation and its MIST tree; the pair
+ * histograms of all systems run in ONE launch over the concatenated tile
+ * list, the trees in one launch (one CTA per system), and the whole device
+ * sequence is captured once into a CUDA graph that later calls with the same
+ * geometry replay. outs (n_sys bodies), edges (n_sys arrays of D_s-1) and
+ * totals (10 per system) may each be NULL. Histogram form only. */
+PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, const int bins[6], int form,
+                            pg_par_body *outs, pg_mist_edge *const *edges, double *totals);
+
 /* Device milliseconds of the kernels of the last pg_entropy / pg_mist call,
  * measured with CUDA events on the context's stream:
  * ms[0] = preprocessing (extrema, modfit, binning, 1D), ms[1] = pair kernel,

@@ -80,6 +80,8 @@ def lib() -> C.CDLL:
         "pg_last_global_error": (cp, []),
         "pg_entropy": (i, [vp, C.POINTER(BatView), C.POINTER(C.c_int), i, C.POINTER(ParBodyC)]),
         "pg_mist": (i, [vp, i, C.POINTER(ParBodyC), C.POINTER(MistEdge), dp]),
+        "pg_entropy_batch": (i, [vp, i, C.POINTER(BatView), C.POINTER(C.c_int), i, C.POINTER(ParBodyC),
+                                 C.POINTER(C.POINTER(MistEdge)), dp]),
         "pg_last_timings": (i, [vp, dp]),
         "pg_launch_count": (i64, [vp]),
         "pg_last_form": (i, [vp]),
@@ -264,6 +266,40 @@ class Engine:
         arr = np.array([(e.type_in, e.type_out, e.index_in, e.index_out, e.mi, e.left) for e in edges[:n]],
                        dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"), ("left", "i4")])
         return arr, np.array(totals[:], dtype=np.float64)
+
+    def entropy_batch(self, trajs, bins=(50,) * 6, form: str | int = "auto", bodies: bool = True,
+                      trees: bool = True):
+        """PARENT.x + get_PAR_MIST.x on many independent trajectories in one
+        run (pg_entropy_batch). bodies: True (allocate), False (no bodies) or
+        a list of ParBody to fill. Returns (bodies, trees): a list of ParBody
+        (or None) and a list of (edges, totals) as Engine.mist returns them
+        (or None)."""
+        views = [t if isinstance(t, BatView) else t.view() for t in trajs]
+        n = len(views)
+        arr = (BatView * n)(*views)
+        b = (C.c_int * 6)(*bins)
+        f = FORMS[form] if isinstance(form, str) else int(form)
+        if isinstance(bodies, (list, tuple)):
+            outs = list(bodies)           # caller's buffers (e.g. in pinned memory)
+        else:
+            outs = [ParBody.empty(v.n_dihedrals) for v in views] if bodies else None
+        oc = (ParBodyC * n)(*[o.c() for o in outs]) if outs else None
+        ebufs = [(MistEdge * max(3 * v.n_dihedrals + 2, 1))() for v in views] if trees else None
+        ep = (C.POINTER(MistEdge) * n)(*[C.cast(e, C.POINTER(MistEdge)) for e in ebufs]) if trees else None
+        totals = np.zeros(10 * n) if trees else None
+        _check(lib().pg_entropy_batch(self._ctx, n, arr, b, f, oc, ep,
+                                      totals.ctypes.data_as(C.POINTER(C.c_double)) if trees else None),
+               self._ctx)
+        res = None
+        if trees:
+            res = []
+            for k, (v, e) in enumerate(zip(views, ebufs)):
+                m = 3 * v.n_dihedrals + 2
+                a = np.array([(x.type_in, x.type_out, x.index_in, x.index_out, x.mi, x.left) for x in e[:m]],
+                             dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"),
+                                    ("left", "i4")])
+                res.append((a, totals[10 * k:10 * k + 10].copy()))
+        return outs, res
 
     def pair_counts(self, traj: Trajectory, bins, pairs, form: str = "hist") -> list[np.ndarray]:
         """Raw 2D histograms of explicit (g1 < g2) pairs from the GPU pair kernel."""

@@ -109,6 +109,11 @@ struct pg_ctx {
     int last_form = 0;
     bool resident = false;  // MI matrix of the last pg_entropy is valid
     SysGeom geo{};
+    // batched runs: one arena for every system's device data, descriptors,
+    // and the CUDA graph of the last batch geometry
+    DevBuf batch, batchmeta;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<int64_t> graph_key;
 };
 
 static int fail(pg_ctx *c, int code, const char *fmt, ...) {
@@ -291,6 +296,9 @@ static int run_hist32(pg_ctx *ctx, const SysGeom &g, const DofArrays &dof, const
     return PG_OK;
 }
 
+static int mist_edges_to_user(pg_ctx *ctx, int n_dihedrals, const double *hmi, const int *hf, const int *ht,
+                              const double *s1, pg_mist_edge *edges, double totals[10]);
+
 extern "C" {
 
 PG_API const char *pg_last_global_error(void) { return g_global_err.c_str(); }
@@ -324,6 +332,9 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn,
                       &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr})
         b->release();
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->batch.release();
+    ctx->batchmeta.release();
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
@@ -547,8 +558,16 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&ms[2], ctx->ev[2], ctx->ev[3]);
     ctx->timings[2] = ms[1];
+    return mist_edges_to_user(ctx, n_dihedrals, hmi.data(), hf.data(), ht.data(), s1.data(), edges, totals);
+}
 
-    // totals in get_PAR_MIST.cpp:279-287 and :663-765 order
+}  // extern "C"
+
+// Device edge triples (MI, In DOF, Out DOF per step) -> pg_mist_edge records
+// and the 10 totals, in get_PAR_MIST.cpp:279-287 and :663-765 order.
+static int mist_edges_to_user(pg_ctx *ctx, int n_dihedrals, const double *hmi, const int *hf, const int *ht,
+                              const double *s1, pg_mist_edge *edges, double totals[10]) {
+    const int nb = n_dihedrals + 2, na = n_dihedrals + 1, nd = n_dihedrals, D = nb + na + nd;
     double tB = 0, tA = 0, tD = 0, tm = 0, tp[6] = {0, 0, 0, 0, 0, 0};
     for (int k = 0; k < nb; k++) tB += s1[k];
     for (int k = 0; k < na; k++) tA += s1[nb + k];
@@ -576,6 +595,8 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     totals[9] = tB + tA + tD - tm;
     return PG_OK;
 }
+
+extern "C" {
 
 PG_API int pg_last_timings(const pg_ctx *ctx, double ms[5]) {
     if (!ctx || !ms) return PG_ERR_ARG;
@@ -656,6 +677,298 @@ PG_API int pg_host_free_pinned(void *ptr) {
 PG_API int pg_synchronize(pg_ctx *ctx) {
     if (!ctx) return PG_ERR_ARG;
     CK(cudaStreamSynchronize(ctx->stream));
+    return PG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- batches
+
+namespace {
+
+// Byte offsets of one system's device data inside the batch arena.
+struct BatchLayout {
+    SysGeom g;
+    int prec = 0;
+    int64_t ld = 0;
+    size_t cols = 0, bins = 0, dof = 0, par = 0, mi = 0, mist = 0, edges = 0;
+    bool own_cols = false;
+};
+
+size_t al256(size_t x) { return (x + 255) / 256 * 256; }
+
+}  // namespace
+
+static int validate_view(pg_ctx *ctx, const pg_bat_view *tv, int k) {
+    if (tv->n_dihedrals < 0 || tv->n_frames < 1 || (tv->double_prec != 0 && tv->double_prec != 1) ||
+        tv->ld < tv->n_frames || !tv->bonds || !tv->angles || (tv->n_dihedrals > 0 && !tv->dihedrals))
+        return fail(ctx, PG_ERR_ARG, "system %d: invalid trajectory view", k);
+    return PG_OK;
+}
+
+extern "C" {
+
+PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, const int bins[6], int form,
+                            pg_par_body *outs, pg_mist_edge *const *edges, double *totals) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (n_sys < 1 || !trajs || !bins) return fail(ctx, PG_ERR_ARG, "need n_sys >= 1 systems and bins");
+    if (form == PG_FORM_ONEHOT)
+        return fail(ctx, PG_ERR_UNSUPPORTED, "batched runs use the histogram form (the faster form at 50 bins)");
+    if (form != PG_FORM_AUTO && form != PG_FORM_HIST) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    for (int k = 0; k < 6; k++) {
+        if (bins[k] < 1) return fail(ctx, PG_ERR_ARG, "bin count %d (index %d) < 1", bins[k], k);
+        if (k >= 3 && bins[k] > PG_MAX_BINS_2D)
+            return fail(ctx, PG_ERR_UNSUPPORTED, "2D bin count %d > %d", bins[k], PG_MAX_BINS_2D);
+        if (k < 3 && bins[k] > 16384) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin count %d > 16384", bins[k]);
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    ctx->resident = false;
+
+    // ---- layout of every system inside one arena
+    std::vector<BatchLayout> sys((size_t)n_sys);
+    size_t off = 0;
+    int maxF = 1, maxD = 1;
+    for (int s = 0; s < n_sys; s++) {
+        const pg_bat_view &v = trajs[s];
+        int rc = validate_view(ctx, &v, s);
+        if (rc) return rc;
+        BatchLayout &L = sys[s];
+        SysGeom &g = L.g;
+        g.n_dih = v.n_dihedrals;
+        g.nb = g.n_dih + 2;
+        g.na = g.n_dih + 1;
+        g.nd = g.n_dih;
+        g.D = g.nb + g.na + g.nd;
+        g.F = v.n_frames;
+        g.ldb = ((int64_t)g.F + 4095) / 4096 * 4096;
+        for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
+        L.prec = v.double_prec;
+        L.own_cols = !v.on_device;
+        L.ld = v.on_device ? v.ld : v.n_frames;
+        if (L.own_cols) {
+            L.cols = off;
+            off = al256(off + (size_t)g.D * g.F * elem_size(v.double_prec));
+        }
+        L.bins = off;
+        off = al256(off + (size_t)g.D * g.ldb);
+        L.dof = off;
+        off = al256(off + (size_t)g.D * (5 * sizeof(double) + sizeof(int)) + 64);
+        L.par = off;
+        off = al256(off + (size_t)par_layout(g.n_dih).total * sizeof(double));
+        L.mi = off;
+        off = al256(off + (size_t)g.D * g.D * sizeof(double));
+        L.mist = off;
+        off = al256(off + mist_scratch_bytes(g.D));
+        L.edges = off;
+        off = al256(off + (size_t)g.D * (sizeof(double) + 2 * sizeof(int)));
+        maxF = std::max(maxF, g.F);
+        maxD = std::max(maxD, g.D);
+    }
+    if (prep_smem_bytes(sys[0].g) > 200 * 1024) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin counts too large");
+    CK(ctx->batch.ensure(off));
+    CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
+    if (ctx->nlogn_max < maxF) {
+        CK(ctx->nlogn.ensure(((size_t)maxF + 1) * sizeof(double)));
+        CK(launch_nlogn_table((double *)ctx->nlogn.p, maxF, st));
+        ctx->launches++;
+        ctx->nlogn_max = maxF;
+    }
+    char *arena = (char *)ctx->batch.p;
+    const int bmax = bmax_of(sys[0].g);
+    int T = 0, fc = 0, nst = 0;
+    if (!pairs_hist_config(bmax, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+
+    // ---- descriptors and the concatenated tile list
+    auto dofs_at = [&](const BatchLayout &L) {
+        DofArrays d;
+        double *b = (double *)(arena + L.dof);
+        const int D = L.g.D;
+        d.mn = b;
+        d.mx = b + D;
+        d.shift = b + 2 * (size_t)D;
+        d.s1 = b + 3 * (size_t)D;
+        d.acon = b + 4 * (size_t)D;
+        d.b2 = (int *)(b + 5 * (size_t)D);
+        return d;
+    };
+    std::vector<SysDesc> sd((size_t)n_sys);
+    std::vector<MistDesc> md((size_t)n_sys);
+    std::vector<PairTile> tiles;
+    std::vector<int> tsys;
+    for (int s = 0; s < n_sys; s++) {
+        const BatchLayout &L = sys[s];
+        sd[s].geo = L.g;
+        sd[s].bins = (const uint8_t *)(arena + L.bins);
+        sd[s].dof = dofs_at(L);
+        sd[s].out.par = (double *)(arena + L.par);
+        sd[s].out.mi = (double *)(arena + L.mi);
+        sd[s].out.L = par_layout(L.g.n_dih);
+        sd[s].out.counts = nullptr;
+        sd[s].out.counts_bmax = 0;
+        sd[s].lnN = log((double)L.g.F);
+        md[s].D = L.g.D;
+        md[s].nb = L.g.nb;
+        md[s].na = L.g.na;
+        md[s].mi = (const double *)(arena + L.mi);
+        md[s].scratch = arena + L.mist;
+        md[s].edge_mi = (double *)(arena + L.edges);
+        md[s].edge_from = (int *)(md[s].edge_mi + L.g.D);
+        md[s].edge_to = md[s].edge_from + L.g.D;
+    }
+    // tiles of the systems with the most frames (the longest tiles) first, so
+    // that the short ones fill the tail of the launch
+    std::vector<int> order((size_t)n_sys);
+    for (int s = 0; s < n_sys; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a].g.F > sys[b].g.F; });
+    for (int s : order) {
+        std::vector<PairTile> t = build_tiles(sys[s].g.D, T);
+        tiles.insert(tiles.end(), t.begin(), t.end());
+        tsys.insert(tsys.end(), t.size(), s);
+    }
+    const size_t mo_sd = 0, mo_md = al256(sizeof(SysDesc) * n_sys), mo_t = mo_md + al256(sizeof(MistDesc) * n_sys),
+                 mo_ts = mo_t + al256(sizeof(PairTile) * std::max<size_t>(tiles.size(), 1)),
+                 mo_end = mo_ts + al256(sizeof(int) * std::max<size_t>(tsys.size(), 1));
+    CK(ctx->batchmeta.ensure(mo_end));
+    char *meta = (char *)ctx->batchmeta.p;
+
+    // the graph depends on the arena/descriptor addresses and geometry; it is
+    // recaptured when any of them change
+    std::vector<int64_t> key = {(int64_t)n_sys, (int64_t)(uintptr_t)arena, (int64_t)(uintptr_t)meta,
+                                (int64_t)(uintptr_t)ctx->nlogn.p, (int64_t)(uintptr_t)ctx->errw.p};
+    for (int k = 0; k < 6; k++) key.push_back(bins[k]);
+    for (int s = 0; s < n_sys; s++) {
+        const pg_bat_view &v = trajs[s];
+        key.insert(key.end(), {v.n_dihedrals, v.n_frames, v.double_prec, v.on_device, v.ld,
+                               v.on_device ? (int64_t)(uintptr_t)v.bonds : 0,
+                               v.on_device ? (int64_t)(uintptr_t)v.angles : 0,
+                               v.on_device ? (int64_t)(uintptr_t)v.dihedrals : 0});
+    }
+    const bool reuse = ctx->graph && key == ctx->graph_key;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    if (!reuse) {
+        CK(cudaMemcpyAsync(meta + mo_sd, sd.data(), sizeof(SysDesc) * n_sys, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(meta + mo_md, md.data(), sizeof(MistDesc) * n_sys, cudaMemcpyHostToDevice, st));
+        if (!tiles.empty()) {
+            CK(cudaMemcpyAsync(meta + mo_t, tiles.data(), sizeof(PairTile) * tiles.size(), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(meta + mo_ts, tsys.data(), sizeof(int) * tsys.size(), cudaMemcpyHostToDevice, st));
+        }
+        CK(cudaStreamSynchronize(st));  // host vectors go out of scope
+    }
+    // host columns -> arena (outside the graph: their source is the caller's)
+    for (int s = 0; s < n_sys; s++) {
+        const BatchLayout &L = sys[s];
+        if (!L.own_cols) continue;
+        const pg_bat_view &v = trajs[s];
+        const size_t es = elem_size(v.double_prec), F = (size_t)v.n_frames;
+        char *dst = arena + L.cols;
+        const void *src[3] = {v.bonds, v.angles, v.dihedrals};
+        const int cnt[3] = {L.g.nb, L.g.na, L.g.nd};
+        for (int t = 0; t < 3; t++) {
+            if (cnt[t] == 0) continue;
+            CK(cudaMemcpy2DAsync(dst, F * es, src[t], (size_t)v.ld * es, F * es, cnt[t], cudaMemcpyHostToDevice, st));
+            dst += (size_t)cnt[t] * F * es;
+        }
+    }
+    CK(cudaEventRecord(ctx->ev[1], st));
+    if (!reuse) {
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st);
+        for (int s = 0; s < n_sys && e == cudaSuccess; s++) {
+            const BatchLayout &L = sys[s];
+            const pg_bat_view &v = trajs[s];
+            const size_t es = elem_size(v.double_prec);
+            const void *cols[3];
+            if (L.own_cols) {
+                const char *c = arena + L.cols;
+                cols[0] = c;
+                cols[1] = c + (size_t)L.g.nb * L.g.F * es;
+                cols[2] = L.g.nd ? c + (size_t)(L.g.nb + L.g.na) * L.g.F * es : cols[1];
+            } else {
+                cols[0] = v.bonds;
+                cols[1] = v.angles;
+                cols[2] = v.dihedrals ? v.dihedrals : v.angles;
+            }
+            const DofArrays d = dofs_at(L);
+            e = launch_prep(L.g, cols, L.ld, L.prec, d, (uint8_t *)(arena + L.bins), (int *)ctx->errw.p, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(arena + L.par, d.s1, (size_t)L.g.D * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        }
+        if (e == cudaSuccess)
+            e = launch_pairs_hist_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
+                                        (const int *)(meta + mo_ts), (int64_t)tiles.size(),
+                                        (const double *)ctx->nlogn.p, (int *)ctx->errw.p, T, st);
+        if (e == cudaSuccess) e = launch_mist_batch((const MistDesc *)(meta + mo_md), n_sys, maxD, st);
+        cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->graph, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->graph = nullptr;
+            return fail(ctx, PG_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+        }
+        ctx->graph_key = key;
+    }
+    CK(cudaGraphLaunch(ctx->graph, st));
+    ctx->launches += n_sys + 2;  // one prep kernel per system, then the pair and MIST kernels
+    CK(cudaEventRecord(ctx->ev[2], st));
+    int rc = check_err_words(ctx);
+    float ms[2];
+    cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);
+    ctx->timings[0] = 0;
+    ctx->timings[1] = ms[1];
+    ctx->timings[2] = 0;
+    ctx->timings[3] = ms[0];
+    ctx->timings[4] = ms[0] + ms[1];
+    if (rc) return rc;
+    ctx->last_form = PG_FORM_HIST;
+
+    // ---- results to the caller
+    for (int s = 0; s < n_sys; s++) {
+        const BatchLayout &L = sys[s];
+        const ParLayout PL = par_layout(L.g.n_dih);
+        if (outs) {
+            pg_par_body &o = outs[s];
+            double *dst[9] = {o.s1_b, o.s1_a, o.s1_d, o.bb, o.ba, o.bd, o.aa, o.ad, o.dd};
+            const int64_t po[10] = {PL.s1b, PL.s1a, PL.s1d, PL.bb, PL.ba, PL.bd, PL.aa, PL.ad, PL.dd, PL.total};
+            for (int k = 0; k < 9; k++) {
+                const int64_t n = po[k + 1] - po[k];
+                if (n <= 0) continue;
+                if (!dst[k]) return fail(ctx, PG_ERR_ARG, "system %d: null output block %d", s, k);
+                CK(cudaMemcpyAsync(dst[k], (double *)(arena + L.par) + po[k], (size_t)n * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st));
+            }
+        }
+        if ((edges && edges[s]) || totals) {
+            const int D = L.g.D;
+            std::vector<double> hmi((size_t)D), s1((size_t)D);
+            std::vector<int> hf((size_t)D), ht((size_t)D);
+            const double *emi = (const double *)(arena + L.edges);
+            const int *ef = (const int *)(emi + D), *et = ef + D;
+            if (D > 1) {
+                CK(cudaMemcpyAsync(hmi.data(), emi, (size_t)(D - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+                CK(cudaMemcpyAsync(hf.data(), ef, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaMemcpyAsync(ht.data(), et, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+            }
+            CK(cudaMemcpyAsync(s1.data(), (const double *)(arena + L.par), (size_t)D * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            std::vector<pg_mist_edge> tmp((size_t)std::max(D - 1, 1));
+            double tt[10];
+            pg_mist_edge *e = (edges && edges[s]) ? edges[s] : tmp.data();
+            rc = mist_edges_to_user(ctx, L.g.n_dih, hmi.data(), hf.data(), ht.data(), s1.data(), e, tt);
+            if (rc) return rc;
+            if (totals) memcpy(totals + 10 * (size_t)s, tt, sizeof tt);
+        }
+    }
+    CK(cudaStreamSynchronize(st));
     return PG_OK;
 }
 

@@ -94,6 +94,16 @@ struct PairOut {
     int64_t *counts;    // debug dump, per tile: 16 pair slots x Bmax^2 (nullptr normally)
     int counts_bmax;
 };
+// One system of a batch, as the batched kernels read it.
+struct SysDesc {
+    SysGeom geo;
+    const uint8_t *bins;
+    DofArrays dof;
+    PairOut out;
+    double lnN;
+};
+cudaError_t launch_pairs_hist_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
+                                    int64_t n_tiles, const double *nlogn, int *err, int tile_dim, cudaStream_t st);
 cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                               const double *nlogn, const PairTile *tiles, int64_t n_tiles,
                               int tile_dim, PairOut out, int *err, cudaStream_t st);
@@ -117,6 +127,17 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
                                 void *scratch, size_t scratch_bytes, int *launches);
 size_t pairs_onehot_scratch_bytes(const SysGeom &g);
 bool pairs_onehot_supported(const SysGeom &g);
+
+// One system of a batched MIST launch (one CTA each); scratch holds
+// key[D] | from[D] | pos[D] (mist_scratch_bytes(D)).
+struct MistDesc {
+    int D, nb, na;
+    const double *mi;
+    void *scratch;
+    double *edge_mi;
+    int *edge_from, *edge_to;
+};
+cudaError_t launch_mist_batch(const MistDesc *sys, int n_sys, int max_D, cudaStream_t st);
 
 // MI matrix from a .par body already on the device (get_mutual semantics).
 cudaError_t launch_mi_from_par(int n_dih, const double *par, ParLayout L, double *mi,

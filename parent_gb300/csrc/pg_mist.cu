@@ -50,9 +50,8 @@ __device__ __forceinline__ bool better(const Cand &a, const Cand &b, const int *
 }
 
 template <bool SMEM>
-__global__ void __launch_bounds__(kThreads, 1)
-mist_kernel(int D, int nb, int na, const double *__restrict__ mi, double *gkey, int *gfrom,
-            int *pos, double *edge_mi, int *edge_from, int *edge_to) {
+__device__ __forceinline__ void mist_body(int D, int nb, int na, const double *__restrict__ mi, double *gkey,
+                                          int *gfrom, int *pos, double *edge_mi, int *edge_from, int *edge_to) {
     extern __shared__ __align__(16) unsigned char smem[];
     double *key = SMEM ? (double *)smem : gkey;
     int *from = SMEM ? (int *)(smem + (size_t)D * sizeof(double)) : gfrom;
@@ -127,6 +126,23 @@ mist_kernel(int D, int nb, int na, const double *__restrict__ mi, double *gkey, 
     }
 }
 
+template <bool SMEM>
+__global__ void __launch_bounds__(kThreads, 1)
+mist_kernel(int D, int nb, int na, const double *__restrict__ mi, double *gkey, int *gfrom,
+            int *pos, double *edge_mi, int *edge_from, int *edge_to) {
+    mist_body<SMEM>(D, nb, na, mi, gkey, gfrom, pos, edge_mi, edge_from, edge_to);
+}
+
+// One CTA per system of a batch.
+template <bool SMEM>
+__global__ void __launch_bounds__(kThreads, 1) mist_batch_kernel(const MistDesc *__restrict__ sys) {
+    const MistDesc &d = sys[blockIdx.x];
+    double *gkey = (double *)d.scratch;
+    int *gfrom = (int *)(gkey + d.D);
+    int *pos = gfrom + d.D;
+    mist_body<SMEM>(d.D, d.nb, d.na, d.mi, gkey, gfrom, pos, d.edge_mi, d.edge_from, d.edge_to);
+}
+
 // Dense symmetric MI matrix from a .par body on the device, get_mutual
 // (util.cpp:47-81): MI = S1[lower] + S1[higher] - S2D.
 __global__ void mi_from_par_kernel(int n_dih, const double *par, ParLayout L, double *mi) {
@@ -163,6 +179,20 @@ cudaError_t launch_mist_impl(int D, int nb, int na, const double *mi, void *scra
     } else {
         mist_kernel<false><<<1, kThreads, 0, st>>>(D, nb, na, mi, gkey, gfrom, pos, edge_mi,
                                                    edge_from, edge_to);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mist_batch(const MistDesc *sys, int n_sys, int max_D, cudaStream_t st) {
+    if (n_sys <= 0) return cudaSuccess;
+    const size_t smem = (size_t)max_D * (sizeof(double) + sizeof(int));
+    if (smem <= 200 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(mist_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        mist_batch_kernel<true><<<n_sys, kThreads, smem, st>>>(sys);
+    } else {
+        mist_batch_kernel<false><<<n_sys, kThreads, 0, st>>>(sys);
     }
     return cudaGetLastError();
 }

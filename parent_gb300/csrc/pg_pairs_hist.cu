@@ -95,11 +95,13 @@ struct TileCfg {
     static constexpr int SHIFT = T == 4 ? 6 : (T == 2 ? 4 : 2);  // log2(PPS * 4)
 };
 
+// One CTA's work on one tile; shared by the single-system kernel and the
+// batched kernel (which reads geometry and outputs per tile from SysDesc).
 template <int T>
-__global__ void __launch_bounds__(kThreads, 1)
-pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
-                  const double *__restrict__ nlogn, const PairTile *__restrict__ tiles,
-                  PairOut out, int *err, int fc, int nst, int bmax, double lnN) {
+__device__ __forceinline__ void pairs_hist_body(const SysGeom &geo, const uint8_t *__restrict__ bins,
+                                                const DofArrays &dof, const double *__restrict__ nlogn,
+                                                const PairTile tile, int64_t tile_index, const PairOut &out,
+                                                int *err, int fc, int nst, int bmax, double lnN) {
     using C = TileCfg<T>;
     constexpr int PPS = C::PPS, NSUB = C::NSUB, NROW = C::NROW;
     constexpr int SH = C::SHIFT;  // log2(bytes between consecutive bins of one slot)
@@ -112,7 +114,6 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
     __shared__ volatile int s_abort;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const PairTile tile = tiles[blockIdx.x];
     const int F = geo.F;
 
     // staged row k: row DOF row0+k (k < T), column DOF col0+k-T (k >= T)
@@ -263,7 +264,7 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
             }
         }
         if (out.counts) {
-            int64_t *dst = out.counts + ((int64_t)blockIdx.x * PPS + ep) * out.counts_bmax * out.counts_bmax;
+            int64_t *dst = out.counts + (tile_index * PPS + ep) * out.counts_bmax * out.counts_bmax;
             for (int bin = ej; bin < nbin; bin += kThreads / PPS) dst[bin] = hist[bin * PPS + ep];
         }
     }
@@ -293,6 +294,25 @@ pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
             out.mi[(int64_t)egc * geo.D + egr] = mi;
         }
     }
+}
+
+template <int T>
+__global__ void __launch_bounds__(kThreads, 1)
+pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
+                  const double *__restrict__ nlogn, const PairTile *__restrict__ tiles,
+                  PairOut out, int *err, int fc, int nst, int bmax, double lnN) {
+    pairs_hist_body<T>(geo, bins, dof, nlogn, tiles[blockIdx.x], blockIdx.x, out, err, fc, nst, bmax, lnN);
+}
+
+// Many independent systems in one launch: tile k belongs to system tile_sys[k].
+template <int T>
+__global__ void __launch_bounds__(kThreads, 1)
+pairs_hist_batch_kernel(const SysDesc *__restrict__ sys, const PairTile *__restrict__ tiles,
+                        const int *__restrict__ tile_sys, const double *__restrict__ nlogn, int *err, int fc,
+                        int nst, int bmax) {
+    const SysDesc &d = sys[tile_sys[blockIdx.x]];
+    pairs_hist_body<T>(d.geo, d.bins, d.dof, nlogn, tiles[blockIdx.x], blockIdx.x, d.out, err, fc, nst, bmax,
+                       d.lnN);
 }
 
 template <int T>
@@ -369,6 +389,24 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
     if (e != cudaSuccess) return e;                                                               \
     pairs_hist_kernel<TT><<<(unsigned)n_tiles, kThreads, smem, st>>>(g, bins, dof, nlogn, tiles,  \
                                                                       out, err, fc, nst, bmax, lnN);
+    if (T == 4) { PG_LAUNCH(4) } else if (T == 2) { PG_LAUNCH(2) } else { PG_LAUNCH(1) }
+#undef PG_LAUNCH
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_hist_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
+                                    int64_t n_tiles, const double *nlogn, int *err, int tile_dim, cudaStream_t st) {
+    int T = 0, fc = 0, nst = 0;
+    const int smem = pairs_hist_config(bmax, &T, &fc, &nst);
+    if (!smem || T != tile_dim) return cudaErrorInvalidValue;
+    if (n_tiles <= 0) return cudaSuccess;
+    cudaError_t e;
+#define PG_LAUNCH(TT)                                                                                    \
+    e = cudaFuncSetAttribute(pairs_hist_batch_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             smem);                                                                     \
+    if (e != cudaSuccess) return e;                                                                     \
+    pairs_hist_batch_kernel<TT><<<(unsigned)n_tiles, kThreads, smem, st>>>(sys, tiles, tile_sys, nlogn, \
+                                                                            err, fc, nst, bmax);
     if (T == 4) { PG_LAUNCH(4) } else if (T == 2) { PG_LAUNCH(2) } else { PG_LAUNCH(1) }
 #undef PG_LAUNCH
     return cudaGetLastError();
