@@ -102,6 +102,9 @@ struct pg_ctx {
     std::string err;
     DevBuf cols, bins, dofbuf, par, mi, nlogn, tiles, errw, scratch, counts, edges, mistscr;
     int nlogn_max = -1;
+    DevBuf nfix;          // fixed-point n ln n table of the histogram kernel
+    int nfix_max = -1;
+    double nfix_scale = 0.0;
     std::vector<PairTile> tiles_host;
     int tiles_D = -1, tiles_T = -1;
     int64_t launches = 0;
@@ -229,6 +232,19 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     return PG_OK;
 }
 
+// Fixed-point n ln n table covering counts up to F. A table built for a
+// larger F is reused: its scale is no larger, so sums still fit 64 bits.
+static int ensure_fix_table(pg_ctx *ctx, int F) {
+    if (ctx->nfix_max >= F) return PG_OK;
+    const double fix = nlogn_fix_scale(F);
+    CK(ctx->nfix.ensure(((size_t)F + 1) * sizeof(unsigned long long)));
+    CK(launch_nlogn_fix_table((unsigned long long *)ctx->nfix.p, F, fix, ctx->stream));
+    ctx->launches++;
+    ctx->nfix_max = F;
+    ctx->nfix_scale = fix;
+    return PG_OK;
+}
+
 static int check_err_words(pg_ctx *ctx) {
     int h[ERR_WORDS];
     CK(cudaMemcpyAsync(h, ctx->errw.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
@@ -329,7 +345,7 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn,
+    for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn, &ctx->nfix,
                       &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr})
         b->release();
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
@@ -388,7 +404,10 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
             ctx->tiles_D = g.D;
             ctx->tiles_T = T;
         }
-        CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const double *)ctx->nlogn.p,
+        int rc3 = ensure_fix_table(ctx, g.F);
+        if (rc3) return rc3;
+        CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                             ctx->nfix_scale,
                              (const PairTile *)ctx->tiles.p, (int64_t)ctx->tiles_host.size(), T, po,
                              (int *)ctx->errw.p, st));
         ctx->launches++;
@@ -471,8 +490,11 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
         CK(ctx->counts.ensure((size_t)n_pairs * pps * bm * bm * sizeof(int64_t)));
         CK(cudaMemcpyAsync(tiles.p, t.data(), t.size() * sizeof(PairTile), cudaMemcpyHostToDevice, st));
         po.counts = (int64_t *)ctx->counts.p;
-        e = launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof_arrays(ctx, g.D), (const double *)ctx->nlogn.p,
-                              (const PairTile *)tiles.p, n_pairs, T, po, (int *)ctx->errw.p, st);
+        int rc3 = ensure_fix_table(ctx, g.F);
+        if (rc3) return rc3;
+        e = launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof_arrays(ctx, g.D),
+                              (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale, (const PairTile *)tiles.p,
+                              n_pairs, T, po, (int *)ctx->errw.p, st);
         ctx->launches++;
     }
     if (e == cudaSuccess) {
@@ -769,11 +791,9 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     if (prep_smem_bytes(sys[0].g) > 200 * 1024) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin counts too large");
     CK(ctx->batch.ensure(off));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
-    if (ctx->nlogn_max < maxF) {
-        CK(ctx->nlogn.ensure(((size_t)maxF + 1) * sizeof(double)));
-        CK(launch_nlogn_table((double *)ctx->nlogn.p, maxF, st));
-        ctx->launches++;
-        ctx->nlogn_max = maxF;
+    {
+        int rc0 = ensure_fix_table(ctx, maxF);
+        if (rc0) return rc0;
     }
     char *arena = (char *)ctx->batch.p;
     const int bmax = bmax_of(sys[0].g);
@@ -836,7 +856,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     // the graph depends on the arena/descriptor addresses and geometry; it is
     // recaptured when any of them change
     std::vector<int64_t> key = {(int64_t)n_sys, (int64_t)(uintptr_t)arena, (int64_t)(uintptr_t)meta,
-                                (int64_t)(uintptr_t)ctx->nlogn.p, (int64_t)(uintptr_t)ctx->errw.p};
+                                (int64_t)(uintptr_t)ctx->nfix.p, (int64_t)(uintptr_t)ctx->errw.p};
+    key.push_back((int64_t)ctx->nfix_max);
     for (int k = 0; k < 6; k++) key.push_back(bins[k]);
     for (int s = 0; s < n_sys; s++) {
         const pg_bat_view &v = trajs[s];
@@ -903,7 +924,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         if (e == cudaSuccess)
             e = launch_pairs_hist_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
                                         (const int *)(meta + mo_ts), (int64_t)tiles.size(),
-                                        (const double *)ctx->nlogn.p, (int *)ctx->errw.p, T, st);
+                                        (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,
+                                        (int *)ctx->errw.p, T, st);
         if (e == cudaSuccess) e = launch_mist_batch((const MistDesc *)(meta + mo_md), n_sys, maxD, st);
         cudaError_t e2 = cudaStreamEndCapture(st, &graph);
         if (e == cudaSuccess) e = e2;

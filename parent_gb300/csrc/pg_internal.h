@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include <vector>
@@ -78,6 +79,9 @@ struct PairTile {
 
 // nlogn[n] = n ln n for n in [0, nmax] (FP64).
 cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st);
+// nfix[n] = round(n ln n * fix) for n in [0, nmax], fix = nlogn_fix_scale(F)
+// for some F >= nmax (fixed point, so sums are exact integer additions).
+cudaError_t launch_nlogn_fix_table(unsigned long long *nfix, int nmax, double fix, cudaStream_t st);
 
 // Extrema + modfit + binning + 1D entropies + 2D decomposition constants.
 // cols[t] = device base of the type-t block (columns ld elements apart).
@@ -102,10 +106,21 @@ struct SysDesc {
     PairOut out;
     double lnN;
 };
+
+// 2^s with s as large as possible (<= 44) such that F ln F * 2^s stays below
+// 1.6e19: sums of n ln n over a histogram of F frames, rounded to multiples
+// of 2^-s, then fit in 64-bit unsigned integers.
+inline double nlogn_fix_scale(int F) {
+    const double top = (double)F * log((double)F > 1 ? (double)F : 2.0) + 1.0;
+    int s = (int)floor(log2(1.6e19 / top));
+    if (s > 44) s = 44;
+    return ldexp(1.0, s);
+}
 cudaError_t launch_pairs_hist_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
-                                    int64_t n_tiles, const double *nlogn, int *err, int tile_dim, cudaStream_t st);
+                                    int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
+                                    int tile_dim, cudaStream_t st);
 cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
-                              const double *nlogn, const PairTile *tiles, int64_t n_tiles,
+                              const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
                               int tile_dim, PairOut out, int *err, cudaStream_t st);
 // smem bytes the histogram kernel needs for a given max 2D bin count, or 0 if
 // it cannot run; sets *tile_dim (4, 2 or 1 DOFs per tile side) and the

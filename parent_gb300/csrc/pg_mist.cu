@@ -14,6 +14,12 @@
 // (type(from), type(v), position(from), v) ascending, i.e. the reference's
 // scan order. One persistent CTA of 1024 threads keeps key/from in shared
 // memory and reads one MI row (the vertex that just joined) per step.
+//
+// MI values are compared as order-preserving 64-bit integer images of the
+// doubles (sign-magnitude flipped to two's-complement order, -0 folded onto
+// +0), so equal doubles give equal keys and every comparison runs on the
+// integer pipe; the FP64 pipe of this part is a small fraction of its
+// integer rate.
 #include <stdint.h>
 
 #include "pg_internal.h"
@@ -26,9 +32,20 @@ constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
 
 struct Cand {
-    double key;
+    unsigned long long key;
     int v;  // -1: none
 };
+
+// order-preserving image of a (non-NaN) double; 0 is below every value
+__device__ __forceinline__ unsigned long long okey(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if (b == 0x8000000000000000ull) b = 0ull;  // -0 == +0
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double okey_value(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
 
 __device__ __forceinline__ int type_of(int g, int nb, int na) { return dof_type(g, nb, na); }
 
@@ -38,7 +55,7 @@ __device__ __forceinline__ bool better(const Cand &a, const Cand &b, const int *
     if (a.v < 0) return false;
     if (b.v < 0) return true;
     if (a.key > b.key) return true;
-    if (a.key < b.key || !(a.key == b.key)) return false;
+    if (a.key < b.key) return false;
     const int fa = from[a.v], fb = from[b.v];
     const int tfa = fa >= 0 ? type_of(fa, nb, na) : 3, tfb = fb >= 0 ? type_of(fb, nb, na) : 3;
     if (tfa != tfb) return tfa < tfb;
@@ -50,18 +67,19 @@ __device__ __forceinline__ bool better(const Cand &a, const Cand &b, const int *
 }
 
 template <bool SMEM>
-__device__ __forceinline__ void mist_body(int D, int nb, int na, const double *__restrict__ mi, double *gkey,
-                                          int *gfrom, int *pos, double *edge_mi, int *edge_from, int *edge_to) {
+__device__ __forceinline__ void mist_body(int D, int nb, int na, const double *__restrict__ mi,
+                                          unsigned long long *gkey, int *gfrom, int *pos, double *edge_mi,
+                                          int *edge_from, int *edge_to) {
     extern __shared__ __align__(16) unsigned char smem[];
-    double *key = SMEM ? (double *)smem : gkey;
-    int *from = SMEM ? (int *)(smem + (size_t)D * sizeof(double)) : gfrom;
+    unsigned long long *key = SMEM ? (unsigned long long *)smem : gkey;
+    int *from = SMEM ? (int *)(smem + (size_t)D * sizeof(unsigned long long)) : gfrom;
     __shared__ Cand wbest[kWarps];
     __shared__ int s_win;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     // In = {bond 0} (get_PAR_MIST.cpp:419-422)
     for (int v = tid; v < D; v += kThreads) {
-        key[v] = -1e200;
+        key[v] = 0ull;
         from[v] = v == 0 ? -2 : -1;  // -2: in the tree, -1: no In partner yet
     }
     if (tid == 0) {
@@ -78,8 +96,8 @@ __device__ __forceinline__ void mist_body(int D, int nb, int na, const double *_
         for (int v = tid; v < D; v += kThreads) {
             const int f = from[v];
             if (f == -2) continue;
-            const double m = __ldg(row + v);
-            const double k = key[v];
+            const unsigned long long m = okey(__ldg(row + v));
+            const unsigned long long k = key[v];
             if (m > k || (m == k && f >= 0 && tw < type_of(f, nb, na))) {
                 key[v] = m;
                 from[v] = w;
@@ -88,7 +106,7 @@ __device__ __forceinline__ void mist_body(int D, int nb, int na, const double *_
         if (step == D - 1) break;
         __syncthreads();
         // argmax in the reference's order
-        Cand best{0.0, -1};
+        Cand best{0ull, -1};
         for (int v = tid; v < D; v += kThreads) {
             if (from[v] == -2) continue;
             const Cand c{key[v], v};
@@ -112,7 +130,7 @@ __device__ __forceinline__ void mist_body(int D, int nb, int na, const double *_
             }
             if (lane == 0) {
                 const int v = b.v < 0 ? 0 : b.v;
-                edge_mi[step] = b.key;
+                edge_mi[step] = okey_value(b.key);
                 edge_from[step] = b.v < 0 ? -1 : from[v];
                 edge_to[step] = b.v;
                 if (b.v >= 0) {
@@ -128,7 +146,7 @@ __device__ __forceinline__ void mist_body(int D, int nb, int na, const double *_
 
 template <bool SMEM>
 __global__ void __launch_bounds__(kThreads, 1)
-mist_kernel(int D, int nb, int na, const double *__restrict__ mi, double *gkey, int *gfrom,
+mist_kernel(int D, int nb, int na, const double *__restrict__ mi, unsigned long long *gkey, int *gfrom,
             int *pos, double *edge_mi, int *edge_from, int *edge_to) {
     mist_body<SMEM>(D, nb, na, mi, gkey, gfrom, pos, edge_mi, edge_from, edge_to);
 }
@@ -137,7 +155,7 @@ mist_kernel(int D, int nb, int na, const double *__restrict__ mi, double *gkey, 
 template <bool SMEM>
 __global__ void __launch_bounds__(kThreads, 1) mist_batch_kernel(const MistDesc *__restrict__ sys) {
     const MistDesc &d = sys[blockIdx.x];
-    double *gkey = (double *)d.scratch;
+    unsigned long long *gkey = (unsigned long long *)d.scratch;
     int *gfrom = (int *)(gkey + d.D);
     int *pos = gfrom + d.D;
     mist_body<SMEM>(d.D, d.nb, d.na, d.mi, gkey, gfrom, pos, d.edge_mi, d.edge_from, d.edge_to);
@@ -166,10 +184,10 @@ size_t mist_scratch_bytes(int D) { return (size_t)D * (sizeof(double) + 2 * size
 
 cudaError_t launch_mist_impl(int D, int nb, int na, const double *mi, void *scratch,
                              double *edge_mi, int *edge_from, int *edge_to, cudaStream_t st) {
-    double *gkey = (double *)scratch;
+    unsigned long long *gkey = (unsigned long long *)scratch;
     int *gfrom = (int *)(gkey + D);
     int *pos = gfrom + D;
-    const size_t smem = (size_t)D * (sizeof(double) + sizeof(int));
+    const size_t smem = (size_t)D * (sizeof(unsigned long long) + sizeof(int));
     if (smem <= 200 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(mist_kernel<true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

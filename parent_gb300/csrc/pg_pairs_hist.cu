@@ -2,88 +2,64 @@
 //
 // Replaces the fifteen 2D fill + epilogue loops of PARENT.cpp (bb :786-823,
 // ba :826-856, bd :858-886, aa :1141-1176, ad :1178-1206, dd :1383-1414 and
-// their remote-rank copies). One CTA owns one pair tile: T row DOFs x T
-// column DOFs (T = 4 -> 16 pairs). Per frame chunk, one elected thread
-// stages the tile's 2T uint8 bin rows into shared memory with bulk TMA copies
-// (cp.async.bulk, completion on an mbarrier; two stages). Every lane owns one
-// pair slot p and a frame sub-stream s; it adds 1 to hist[(br*Bc + bc)*PPS + p]
-// with a shared-memory reduction, so the PPS pair histograms are interleaved
-// word by word and lanes of different pairs never share a bank.
+// their remote-rank copies). A pair tile is T row DOFs x T column DOFs
+// (T = 4 -> 16 pairs). The kernel is persistent: one CTA per SM walks the
+// tile list with a stride of the grid size, so the CTA's shared-memory
+// histograms, barriers and staging ring live across tiles.
 //
-// The epilogue reduces each histogram to sum n ln n (FP64 table lookup) and
-// the occupied-bin count, then forms the 2D entropy through the exact
-// decomposition
+// Warp 31 is the producer: one lane streams every chunk of every tile of the
+// CTA, the tile's 2T uint8 bin rows per chunk, into a ring of shared-memory
+// stages with bulk TMA copies (cp.async.bulk, completion on a full[] mbarrier)
+// and refills a stage once every consumer warp has released it (empty[]). It
+// runs ahead into the next tile while the consumers finish the current one,
+// so no tile starts with an empty pipeline.
+//
+// Warps 0-30 consume: every lane owns one pair slot p and a frame sub-stream
+// and adds 1 to hist[(br*Bc + bc)*PPS + p] with a shared-memory reduction, so
+// the PPS pair histograms are interleaved word by word and lanes of different
+// pairs never share a bank.
+//
+// Epilogue (consumers only, per tile): each histogram is reduced to
+// sum n ln n and the occupied bin count while the words are reset to zero
+// for the next tile. n ln n comes from a fixed-point table (n ln n * 2^s, s
+// chosen from F so that any histogram's total stays below 2^64): the sums
+// are 64-bit integer additions, exact and independent of the order the warps
+// arrive in, and they keep the FP64 pipe (a small fraction of the integer
+// rate on this part) out of the per-bin work. The
+// 2D entropy then follows from the exact decomposition
 //   S_ij = ln N + A_i + A_j - (1/N) sum n ln n + (occ - 1) / (2N)
-// (A from the preprocessing kernel), the mutual information
-//   MI = S1_i + S1_j - S_ij   (get_mutual, util.cpp:47-81)
-// and writes S_ij into the .par body layout and MI into the dense matrix.
-// No histogram ever reaches global memory.
+// (A from the preprocessing kernel), the mutual information from
+//   MI = S1_i + S1_j - S_ij   (get_mutual, util.cpp:47-81),
+// S_ij goes into the .par body layout and MI into the dense matrix. No
+// histogram ever reaches global memory.
 #include <stdio.h>
 #include <stdlib.h>
 
 #include "pg_internal.h"
+#include "pg_sync.cuh"
 
 namespace pg {
 
 namespace {
 
+using namespace dev;
+
 constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
+constexpr int kConsumers = kWarps - 1;           // warps 0..30
+constexpr int kConsumerThreads = kConsumers * 32;
 constexpr int kMaxStages = 4;
 constexpr int kSmemMax = 232448;   // 227 KB opt-in per block on sm_100-class parts
 constexpr int kStagePad = 32;      // bytes between staged rows: puts the 2T rows on distinct banks
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz, then report a timeout
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Relaxed arrive: a consumer warp releases a stage after the values it read
-// from it have been used, without waiting for its own shared-memory
-// reductions (which never touch the stage) to drain.
-__device__ __forceinline__ void mbar_arrive_relaxed(uint32_t bar) {
-    asm volatile("mbarrier.arrive.relaxed.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-// Bounded wait: gives up after kWaitCycles and returns false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-        "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
-}
 
 __host__ __device__ __forceinline__ size_t hist_bytes(int bmax, int pps) {
     return ((size_t)bmax * bmax * pps * 4 + 127) / 128 * 128;
 }
 
-// hist[word] += 1 in shared memory, result unused
+// hist[word] += 1 in shared memory, result unused; ordering with the stage
+// release and the barriers comes from those instructions' own clobbers
 __device__ __forceinline__ void red_add1_at(uint32_t saddr) {
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr));  // ordering comes from the arrive/barrier clobbers
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr));
 }
 __device__ __forceinline__ void red_add1(unsigned int *p) { red_add1_at(smem_u32(p)); }
 
@@ -95,231 +71,289 @@ struct TileCfg {
     static constexpr int SHIFT = T == 4 ? 6 : (T == 2 ? 4 : 2);  // log2(PPS * 4)
 };
 
-// One CTA's work on one tile; shared by the single-system kernel and the
-// batched kernel (which reads geometry and outputs per tile from SysDesc).
+// Launch arguments. A single-system launch passes its system in `one` and
+// tile_sys = nullptr; a batched launch passes per-tile system indices into
+// `many`.
+struct HistArgs {
+    SysDesc one;
+    const SysDesc *many;
+    const PairTile *tiles;
+    const int *tile_sys;
+    int64_t n_tiles;
+    const unsigned long long *nfix;
+    double fix;
+    int *err;
+    int fc, nst, bmax;
+};
+
 template <int T>
-__device__ __forceinline__ void pairs_hist_body(const SysGeom &geo, const uint8_t *__restrict__ bins,
-                                                const DofArrays &dof, const double *__restrict__ nlogn,
-                                                const PairTile tile, int64_t tile_index, const PairOut &out,
-                                                int *err, int fc, int nst, int bmax, double lnN) {
+__global__ void __launch_bounds__(kThreads, 1) pairs_hist_kernel(const __grid_constant__ HistArgs a) {
     using C = TileCfg<T>;
     constexpr int PPS = C::PPS, NSUB = C::NSUB, NROW = C::NROW;
     constexpr int SH = C::SHIFT;  // log2(bytes between consecutive bins of one slot)
+    constexpr int NJ = kConsumerThreads / PPS;  // epilogue threads per slot
     extern __shared__ __align__(128) unsigned char smem[];
-    const int hist_words = bmax * bmax * PPS;
+    const int fc = a.fc, nst = a.nst;
+    const int hist_words = a.bmax * a.bmax * PPS;
     unsigned int *hist = (unsigned int *)smem;
     const int fcs = fc + kStagePad;
-    unsigned char *stage = smem + hist_bytes(bmax, PPS);  // [nst][NROW][fcs], 128-B aligned
-    uint64_t *mbar = (uint64_t *)(stage + (size_t)nst * NROW * fcs);
-    __shared__ volatile int s_abort;
+    unsigned char *stage = smem + hist_bytes(a.bmax, PPS);  // [nst][NROW][fcs], 128-B aligned
+    uint64_t *full = (uint64_t *)(stage + (size_t)nst * NROW * fcs);
+    uint64_t *empty = full + kMaxStages;
+    __shared__ unsigned long long s_snl[PPS];
+    __shared__ unsigned int s_occ[PPS];
+    __shared__ volatile int s_abort;    // written by consumers only (read by all after a barrier)
+    __shared__ volatile int s_pabort;   // written by the producer
+    __shared__ long long s_issued;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = geo.F;
-
-    // staged row k: row DOF row0+k (k < T), column DOF col0+k-T (k >= T)
-    auto row_dof = [&](int k) -> int {
-        if (k < T) return k < tile.nrow ? tile.row0 + k : -1;
-        return (k - T) < tile.ncol ? tile.col0 + (k - T) : -1;
-    };
 
     for (int i = tid * 4; i < hist_words; i += kThreads * 4) {
         if (i + 4 <= hist_words) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
         else for (int k = i; k < hist_words; k++) hist[k] = 0u;
     }
+    if (tid < PPS) {
+        s_snl[tid] = 0ull;
+        s_occ[tid] = 0u;
+    }
     if (tid == 0) {
         s_abort = 0;
+        s_pabort = 0;
+        s_issued = 0;
         for (int k = 0; k < nst; k++) {
-            mbar_init(smem_u32(&mbar[k]), 1);                            // full[k]: producer + tx bytes
-            mbar_init(smem_u32(&mbar[kMaxStages + k]), kWarps - 1);      // empty[k]: one per consumer warp
+            mbar_init(smem_u32(&full[k]), 1);             // producer arrival + tx bytes
+            mbar_init(smem_u32(&empty[k]), kConsumers);   // one arrival per consumer warp
         }
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
     }
     __syncthreads();
 
-    const int nchunks = (F + fc - 1) / fc;
-    // Warp-specialised pipeline: warp kWarps-1 is the producer (one lane
-    // issues the bulk copies); warps 0..kWarps-2 consume. full[st] completes
-    // when a stage's bytes have landed; empty[st] when every consumer warp is
-    // done reading it. No CTA-wide barrier inside the loop, so the warps'
-    // in-flight shared-memory reductions never have to drain together.
-    constexpr int kConsumers = kWarps - 1;
-    uint64_t *full = mbar, *empty = mbar + kMaxStages;
+    auto sys_of = [&](int64_t t) -> const SysDesc & { return a.tile_sys ? a.many[a.tile_sys[t]] : a.one; };
+
     if (warp == kConsumers) {
+        // ---------------------------------------------------------- producer
         if (lane == 0) {
-            for (int chunk = 0; chunk < nchunks; chunk++) {
-                const int st = chunk % nst;
-                if (chunk >= nst &&
-                    !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((chunk / nst) - 1) & 1))) {
+            long long seq = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
+                const SysDesc &d = sys_of(t);
+                const PairTile tile = a.tiles[t];
+                const int nchunks = (d.geo.F + fc - 1) / fc;
+                const uint8_t *src[NROW];
+                uint32_t bytes = 0;
+                for (int k = 0; k < NROW; k++) {
+                    const int g = k < T ? (k < tile.nrow ? tile.row0 + k : -1)
+                                        : ((k - T) < tile.ncol ? tile.col0 + (k - T) : -1);
+                    src[k] = g >= 0 ? d.bins + (int64_t)g * d.geo.ldb : nullptr;
+                    bytes += g >= 0 ? (uint32_t)fc : 0u;
+                }
+                for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
+                    const int st = (int)(seq % nst);
+                    if (seq >= nst &&
+                        !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((seq / nst) - 1) & 1))) {
+                        s_pabort = 1;
+                        ok = false;
+                        break;
+                    }
+                    if (s_abort) {  // the consumers gave up: stop issuing
+                        ok = false;
+                        break;
+                    }
+                    // generic-proxy reads of this stage (released by the
+                    // empty barrier) before the async-proxy writes refilling it
+                    fence_proxy_async();
+                    const uint32_t bar = smem_u32(&full[st]);
+                    mbar_expect_tx(bar, bytes);
+                    for (int k = 0; k < NROW; k++) {
+                        if (!src[k]) continue;
+                        bulk_g2s(smem_u32(stage + (size_t)(st * NROW + k) * fcs), src[k] + (int64_t)chunk * fc,
+                                 (uint32_t)fc, bar);
+                    }
+                }
+            }
+            s_issued = seq;
+        }
+    } else {
+        // --------------------------------------------------------- consumers
+        const int p = lane % PPS, sub = lane / PPS;
+        const int pr = p / T, pc = p % T;
+        const uint32_t hbase = smem_u32(hist + p);
+        constexpr int S = kConsumers * NSUB;
+        const int gstep = (fc / 16) % S;
+        const int ctid = tid;  // 0 .. kConsumerThreads-1
+        const int ep = ctid % PPS, ej = ctid / PPS;
+        const int er = ep / T, ec = ep % T;
+        long long seq = 0;
+        for (int64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+            const SysDesc &d = sys_of(t);
+            const PairTile tile = a.tiles[t];
+            const int F = d.geo.F;
+            const int nchunks = (F + fc - 1) / fc;
+            const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
+            const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
+            const bool valid = gr >= 0 && gc >= 0 && gr < gc;
+            const uint32_t Bc = valid ? (uint32_t)d.dof.b2[gc] : 0u;
+            // 16-frame groups go round-robin over the S (warp, sub-stream)
+            // slots; each chunk starts one chunk's group count further along,
+            // so the leftover groups rotate over the warps
+            int g0 = warp * NSUB + sub;
+            for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
+                const int st = (int)(seq % nst);
+                if (!mbar_wait_bounded(smem_u32(&full[st]), (uint32_t)((seq / nst) & 1))) {
                     s_abort = 1;
                     break;
                 }
-                // generic-proxy reads of this stage (released by the empty
-                // barrier) before the async-proxy writes that refill it
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                uint32_t bytes = 0;
-                for (int k = 0; k < NROW; k++) bytes += row_dof(k) >= 0 ? (uint32_t)fc : 0u;
-                const uint32_t bar = smem_u32(&full[st]);
-                mbar_expect_tx(bar, bytes);
-                for (int k = 0; k < NROW; k++) {
-                    const int g = row_dof(k);
-                    if (g < 0) continue;
-                    bulk_g2s(smem_u32(stage + (size_t)(st * NROW + k) * fcs),
-                             bins + (int64_t)g * geo.ldb + (int64_t)chunk * fc, (uint32_t)fc, bar);
-                }
-            }
-        }
-    } else {
-        // this lane's pair slot
-        const int p = lane % PPS, sub = lane / PPS;
-        const int pr = p / T, pc = p % T;
-        const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
-        const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
-        const bool valid = gr >= 0 && gc >= 0 && gr < gc;
-        const uint32_t Bc = valid ? (uint32_t)dof.b2[gc] : 0u;
-        const uint32_t hbase = smem_u32(hist + p);
-        // 16-frame groups go round-robin over the S (warp, sub-stream) slots;
-        // each chunk starts one chunk's group count further along, so the
-        // leftover groups rotate over the warps instead of always landing on
-        // the first ones
-        constexpr int S = kConsumers * NSUB;
-        const int gstep = (fc / 16) % S;
-        int g0 = warp * NSUB + sub;
-        for (int chunk = 0; chunk < nchunks; chunk++) {
-            const int st = chunk % nst;
-            if (!mbar_wait_bounded(smem_u32(&full[st]), (uint32_t)((chunk / nst) & 1))) {
-                s_abort = 1;
-                break;
-            }
-            const int fvalid = min(fc, F - chunk * fc);
-            const unsigned char *rrow = stage + (size_t)(st * NROW + pr) * fcs;
-            const unsigned char *crow = stage + (size_t)(st * NROW + T + pc) * fcs;
-            if (valid) {
-                for (int off = g0 * 16; off < fvalid; off += S * 16) {
-                    const uint4 rv = *(const uint4 *)(rrow + off);
-                    const uint4 cv = *(const uint4 *)(crow + off);
-                    const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
-                    const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
-                    if (off + 16 <= fvalid) {
-                        // two frames per 32-bit IMAD: bytes spread into 16-bit
-                        // halves, idx = br*Bc + bc < 65536 never carries across
+                const int fvalid = min(fc, F - chunk * fc);
+                const unsigned char *rrow = stage + (size_t)(st * NROW + pr) * fcs;
+                const unsigned char *crow = stage + (size_t)(st * NROW + T + pc) * fcs;
+                if (valid) {
+                    for (int off = g0 * 16; off < fvalid; off += S * 16) {
+                        const uint4 rv = *(const uint4 *)(rrow + off);
+                        const uint4 cv = *(const uint4 *)(crow + off);
+                        const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                        const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                        if (off + 16 <= fvalid) {
+                            // two frames per 32-bit IMAD: bytes spread into
+                            // 16-bit halves, idx = br*Bc + bc < 65536 never
+                            // carries across
 #pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            const uint32_t i01 = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
-                            const uint32_t i23 = __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
-                            red_add1_at(hbase + ((i01 & 0xffffu) << SH));
-                            red_add1_at(hbase + ((i01 >> 16) << SH));
-                            red_add1_at(hbase + ((i23 & 0xffffu) << SH));
-                            red_add1_at(hbase + ((i23 >> 16) << SH));
-                        }
-                    } else {  // ragged end of the trajectory
-                        const int n = fvalid - off;
+                            for (int q = 0; q < 4; q++) {
+                                const uint32_t i01 =
+                                    __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
+                                const uint32_t i23 =
+                                    __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
+                                red_add1_at(hbase + ((i01 & 0xffffu) << SH));
+                                red_add1_at(hbase + ((i01 >> 16) << SH));
+                                red_add1_at(hbase + ((i23 & 0xffffu) << SH));
+                                red_add1_at(hbase + ((i23 >> 16) << SH));
+                            }
+                        } else {  // ragged end of the trajectory
+                            const int n = fvalid - off;
 #pragma unroll
-                        for (int k = 0; k < 16; k++) {
-                            if (k < n) {
-                                const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                                const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                                red_add1_at(hbase + ((br * Bc + bc) << SH));
+                            for (int k = 0; k < 16; k++) {
+                                if (k < n) {
+                                    const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                    const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                    red_add1_at(hbase + ((br * Bc + bc) << SH));
+                                }
                             }
                         }
                     }
                 }
+                __syncwarp();
+                if (lane == 0) mbar_arrive_relaxed(smem_u32(&empty[st]));
+                g0 -= gstep;
+                if (g0 < 0) g0 += S;
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive_relaxed(smem_u32(&empty[st]));
-            g0 -= gstep;
-            if (g0 < 0) g0 += S;
+            // every consumer's reductions for this tile are done
+            named_barrier(kConsumerThreads);
+            if (s_abort) break;  // the same value for every consumer (no writes until the next tile)
+
+            // ---- epilogue: sum n ln n and occupied bins per slot; zero the
+            // words for the next tile
+            const int egr = er < tile.nrow ? tile.row0 + er : -1;
+            const int egc = ec < tile.ncol ? tile.col0 + ec : -1;
+            const bool evalid = egr >= 0 && egc >= 0 && egr < egc;
+            unsigned long long snl = 0ull;
+            int occ = 0;
+            if (evalid) {
+                const int nbin = d.dof.b2[egr] * d.dof.b2[egc];
+                unsigned int *h = hist + ep;
+                if (d.out.counts) {
+                    int64_t *dst = d.out.counts + (t * PPS + ep) * d.out.counts_bmax * d.out.counts_bmax;
+                    for (int bin = ej; bin < nbin; bin += NJ) dst[bin] = h[bin * PPS];
+                }
+                int bin = ej;
+                for (; bin + 3 * NJ < nbin; bin += 4 * NJ) {
+                    const unsigned int n0 = h[bin * PPS], n1 = h[(bin + NJ) * PPS];
+                    const unsigned int n2 = h[(bin + 2 * NJ) * PPS], n3 = h[(bin + 3 * NJ) * PPS];
+                    h[bin * PPS] = 0u;
+                    h[(bin + NJ) * PPS] = 0u;
+                    h[(bin + 2 * NJ) * PPS] = 0u;
+                    h[(bin + 3 * NJ) * PPS] = 0u;
+                    snl += __ldg(a.nfix + n0) + __ldg(a.nfix + n1) + __ldg(a.nfix + n2) + __ldg(a.nfix + n3);
+                    occ += (n0 != 0u) + (n1 != 0u) + (n2 != 0u) + (n3 != 0u);
+                }
+                for (; bin < nbin; bin += NJ) {
+                    const unsigned int n = h[bin * PPS];
+                    h[bin * PPS] = 0u;
+                    snl += __ldg(a.nfix + n);
+                    occ += n != 0u;
+                }
+            }
+            // lanes l and l+PPS*k of a warp hold the same slot: fold them
+            for (int o = 16; o >= PPS; o >>= 1) {
+                snl += __shfl_down_sync(0xffffffffu, snl, o);
+                occ += __shfl_down_sync(0xffffffffu, occ, o);
+            }
+            if (lane < PPS && evalid) {
+                atomicAdd(&s_snl[ep], snl);
+                atomicAdd(&s_occ[ep], (unsigned int)occ);
+            }
+            named_barrier(kConsumerThreads);
+            if (ctid < PPS) {
+                if (evalid) {
+                    const double N = (double)F;
+                    const double s = (double)s_snl[ctid] / a.fix;
+                    const int o = (int)s_occ[ctid];
+                    const double S2 = d.lnN + d.dof.acon[egr] + d.dof.acon[egc] - s / N + (o - 1.0) / (2.0 * N);
+                    if (d.out.par) d.out.par[par_pair_index(d.out.L, d.geo.nb, d.geo.na, d.geo.nd, egr, egc)] = S2;
+                    if (d.out.mi) {
+                        const double mi = d.dof.s1[egr] + d.dof.s1[egc] - S2;
+                        d.out.mi[(int64_t)egr * d.geo.D + egc] = mi;
+                        d.out.mi[(int64_t)egc * d.geo.D + egr] = mi;
+                    }
+                }
+                // the next tile's atomics follow its streaming barrier
+                s_snl[ctid] = 0ull;
+                s_occ[ctid] = 0u;
+            }
         }
     }
     __syncthreads();
 
-    if (s_abort) {
-        // a stage never completed: record it, drain every copy that may still
-        // be in flight (bounded), and leave without writing results
+    if (s_abort || s_pabort) {
+        // a wait ran out: record it, let every copy that may still be in
+        // flight land (bounded), and leave
         if (tid == 0) {
-            atomicAdd(&err[ERR_TIMEOUT], 1);
-            for (int c = 0; c < nst; c++) (void)mbar_wait_bounded(smem_u32(&full[c]), 0u);
+            atomicAdd(&a.err[ERR_TIMEOUT], 1);
+            const long long n = s_issued;
+            for (long long k = n > nst ? n - nst : 0; k < n; k++)
+                (void)mbar_wait_bounded(smem_u32(&full[k % nst]), (uint32_t)((k / nst) & 1));
         }
         __syncthreads();
-        return;
     }
-
-    // ---- epilogue: per pair slot, sum n ln n and occupied bins. The staging
-    // area is free now and holds the cross-warp partial sums.
-    double *red_snl = (double *)stage;               // [kWarps][PPS]
-    int *red_occ = (int *)(red_snl + kWarps * PPS);  // [kWarps][PPS]
-    const int ep = tid % PPS, ej = tid / PPS;  // kThreads/PPS threads per slot
-    const int er = ep / T, ec = ep % T;
-    const int egr = er < tile.nrow ? tile.row0 + er : -1;
-    const int egc = ec < tile.ncol ? tile.col0 + ec : -1;
-    const bool evalid = egr >= 0 && egc >= 0 && egr < egc;
-    double snl = 0.0;
-    int occ = 0;
-    if (evalid) {
-        const int nbin = dof.b2[egr] * dof.b2[egc];
-        for (int bin = ej; bin < nbin; bin += kThreads / PPS) {
-            const unsigned int n = hist[bin * PPS + ep];
-            if (n) {
-                snl += __ldg(nlogn + n);
-                occ++;
-            }
-        }
-        if (out.counts) {
-            int64_t *dst = out.counts + (tile_index * PPS + ep) * out.counts_bmax * out.counts_bmax;
-            for (int bin = ej; bin < nbin; bin += kThreads / PPS) dst[bin] = hist[bin * PPS + ep];
-        }
-    }
-    // lanes l and l+PPS*k of a warp hold the same slot: fold them first
-    for (int o = 16; o >= PPS; o >>= 1) {
-        snl += __shfl_down_sync(0xffffffffu, snl, o);
-        occ += __shfl_down_sync(0xffffffffu, occ, o);
-    }
-    if (lane < PPS) {
-        red_snl[warp * PPS + lane] = snl;
-        red_occ[warp * PPS + lane] = occ;
-    }
-    __syncthreads();
-    if (tid < PPS && evalid) {
-        double s = 0.0;
-        int o = 0;
-        for (int w = 0; w < kWarps; w++) {
-            s += red_snl[w * PPS + tid];
-            o += red_occ[w * PPS + tid];
-        }
-        const double N = (double)F;
-        const double S2 = lnN + dof.acon[egr] + dof.acon[egc] - s / N + (o - 1.0) / (2.0 * N);
-        if (out.par) out.par[par_pair_index(out.L, geo.nb, geo.na, geo.nd, egr, egc)] = S2;
-        if (out.mi) {
-            const double mi = dof.s1[egr] + dof.s1[egc] - S2;
-            out.mi[(int64_t)egr * geo.D + egc] = mi;
-            out.mi[(int64_t)egc * geo.D + egr] = mi;
-        }
-    }
-}
-
-template <int T>
-__global__ void __launch_bounds__(kThreads, 1)
-pairs_hist_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
-                  const double *__restrict__ nlogn, const PairTile *__restrict__ tiles,
-                  PairOut out, int *err, int fc, int nst, int bmax, double lnN) {
-    pairs_hist_body<T>(geo, bins, dof, nlogn, tiles[blockIdx.x], blockIdx.x, out, err, fc, nst, bmax, lnN);
-}
-
-// Many independent systems in one launch: tile k belongs to system tile_sys[k].
-template <int T>
-__global__ void __launch_bounds__(kThreads, 1)
-pairs_hist_batch_kernel(const SysDesc *__restrict__ sys, const PairTile *__restrict__ tiles,
-                        const int *__restrict__ tile_sys, const double *__restrict__ nlogn, int *err, int fc,
-                        int nst, int bmax) {
-    const SysDesc &d = sys[tile_sys[blockIdx.x]];
-    pairs_hist_body<T>(d.geo, d.bins, d.dof, nlogn, tiles[blockIdx.x], blockIdx.x, d.out, err, fc, nst, bmax,
-                       d.lnN);
 }
 
 template <int T>
 size_t smem_bytes(int bmax, int fc, int nst) {
     const size_t stage = (size_t)nst * TileCfg<T>::NROW * (fc + kStagePad);
-    const size_t scratch = (size_t)kWarps * TileCfg<T>::PPS * (sizeof(double) + sizeof(int));
-    return hist_bytes(bmax, TileCfg<T>::PPS) + (stage > scratch ? stage : scratch) + 8 * 2 * kMaxStages;
+    return hist_bytes(bmax, TileCfg<T>::PPS) + stage + 8 * 2 * kMaxStages;
+}
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int T>
+cudaError_t launch_t(const HistArgs &a, int smem, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(pairs_hist_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int64_t grid = a.n_tiles < sm_count() ? a.n_tiles : sm_count();
+    pairs_hist_kernel<T><<<(unsigned)grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_any(const HistArgs &a, int T, int smem, cudaStream_t st) {
+    if (T == 4) return launch_t<4>(a, smem, st);
+    if (T == 2) return launch_t<2>(a, smem, st);
+    return launch_t<1>(a, smem, st);
 }
 
 }  // namespace
@@ -356,7 +390,9 @@ int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages) {
             return T == 4 ? smem_bytes<4>(bmax, fc, nst)
                           : (T == 2 ? smem_bytes<2>(bmax, fc, nst) : smem_bytes<1>(bmax, fc, nst));
         };
-        const bool ovr = ofc >= 512 && ofc <= 8192 && ofc % 512 == 0 && onst >= 2 && onst <= kMaxStages;
+        // chunk sizes divide 4096, the padding of every bin row, so the last
+        // chunk never reads past its row
+        const bool ovr = ofc >= 512 && ofc <= 4096 && 4096 % ofc == 0 && onst >= 2 && onst <= kMaxStages;
         if (ovr && need(ofc, onst) + 1024 <= (size_t)kSmemMax) {
             *tile_dim = T; *chunk_frames = ofc; *stages = onst;
             return (int)need(ofc, onst);
@@ -372,7 +408,7 @@ int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages) {
 }
 
 cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
-                              const double *nlogn, const PairTile *tiles, int64_t n_tiles,
+                              const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
                               int tile_dim, PairOut out, int *err, cudaStream_t st) {
     int bmax = 1;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
@@ -381,35 +417,44 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
     if (!smem || T != tile_dim) return cudaErrorInvalidValue;
     if (n_tiles <= 0) return cudaSuccess;
     if ((int64_t)g.ldb < (int64_t)((g.F + fc - 1) / fc) * fc) return cudaErrorInvalidValue;
-    const double lnN = log((double)g.F);
-    cudaError_t e;
-#define PG_LAUNCH(TT)                                                                              \
-    e = cudaFuncSetAttribute(pairs_hist_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             smem);                                                               \
-    if (e != cudaSuccess) return e;                                                               \
-    pairs_hist_kernel<TT><<<(unsigned)n_tiles, kThreads, smem, st>>>(g, bins, dof, nlogn, tiles,  \
-                                                                      out, err, fc, nst, bmax, lnN);
-    if (T == 4) { PG_LAUNCH(4) } else if (T == 2) { PG_LAUNCH(2) } else { PG_LAUNCH(1) }
-#undef PG_LAUNCH
-    return cudaGetLastError();
+    HistArgs a{};
+    a.one.geo = g;
+    a.one.bins = bins;
+    a.one.dof = dof;
+    a.one.out = out;
+    a.one.lnN = log((double)g.F);
+    a.many = nullptr;
+    a.tiles = tiles;
+    a.tile_sys = nullptr;
+    a.n_tiles = n_tiles;
+    a.nfix = nfix;
+    a.fix = fix;
+    a.err = err;
+    a.fc = fc;
+    a.nst = nst;
+    a.bmax = bmax;
+    return launch_any(a, T, smem, st);
 }
 
 cudaError_t launch_pairs_hist_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
-                                    int64_t n_tiles, const double *nlogn, int *err, int tile_dim, cudaStream_t st) {
+                                    int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
+                                    int tile_dim, cudaStream_t st) {
     int T = 0, fc = 0, nst = 0;
     const int smem = pairs_hist_config(bmax, &T, &fc, &nst);
     if (!smem || T != tile_dim) return cudaErrorInvalidValue;
     if (n_tiles <= 0) return cudaSuccess;
-    cudaError_t e;
-#define PG_LAUNCH(TT)                                                                                    \
-    e = cudaFuncSetAttribute(pairs_hist_batch_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             smem);                                                                     \
-    if (e != cudaSuccess) return e;                                                                     \
-    pairs_hist_batch_kernel<TT><<<(unsigned)n_tiles, kThreads, smem, st>>>(sys, tiles, tile_sys, nlogn, \
-                                                                            err, fc, nst, bmax);
-    if (T == 4) { PG_LAUNCH(4) } else if (T == 2) { PG_LAUNCH(2) } else { PG_LAUNCH(1) }
-#undef PG_LAUNCH
-    return cudaGetLastError();
+    HistArgs a{};
+    a.many = sys;
+    a.tiles = tiles;
+    a.tile_sys = tile_sys;
+    a.n_tiles = n_tiles;
+    a.nfix = nfix;
+    a.fix = fix;
+    a.err = err;
+    a.fc = fc;
+    a.nst = nst;
+    a.bmax = bmax;
+    return launch_any(a, T, smem, st);
 }
 
 double probe_smem_red_rate(int n_sm, cudaStream_t st, int *launches) {

@@ -54,15 +54,6 @@ constexpr int kOffBins = (kOffPsOcc + kMaxRowDofs * kMaxColDofs * 4 + 127) / 128
 constexpr int kSmemBytes = kOffBins + 2 * kBinBufBytes;
 constexpr long long kWaitCycles = 4000000000LL;
 // Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
-// F ln F * 2^s < 1.6e19, so a pair's sum of n ln n (at most F ln F) fits in
-// an unsigned 64-bit accumulator; the rounding error per occupied bin is
-// 2^-(s+1), i.e. <= 1.2e-13 at 500,000 frames.
-static double fix_scale(int F) {
-    const double top = (double)F * log((double)F > 1 ? (double)F : 2.0) + 1.0;
-    int s = (int)floor(log2(1.6e19 / top));
-    if (s > 44) s = 44;
-    return ldexp(1.0, s);
-}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -404,11 +395,6 @@ __global__ void onehot_finalize(SysGeom geo, DofArrays dof, const unsigned long 
     }
 }
 
-__global__ void nlogn_fix_kernel(int64_t *t, int nmax, double fix) {
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
-        t[n] = n > 1 ? (int64_t)llrint((double)n * log((double)n) * fix) : 0;
-}
-
 __global__ void rowinfo_kernel(const int *b2, int D, const int64_t *rowstart, uint32_t *rowinfo) {
     const int g = blockIdx.x;
     for (int b = threadIdx.x; b < b2[g]; b += blockDim.x) rowinfo[rowstart[g] + b] = ((uint32_t)g << 8) | (uint32_t)b;
@@ -492,8 +478,8 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
     if ((e = cudaMemsetAsync(d_snl, 0, sizeof(unsigned long long) * (size_t)g.D * g.D, st))) return e;
     if ((e = cudaMemsetAsync(d_occ, 0, sizeof(unsigned int) * (size_t)g.D * g.D, st))) return e;
     rowinfo_kernel<<<g.D, 64, 0, st>>>(dof.b2, g.D, d_rs, d_ri);
-    const double fix = fix_scale(g.F);
-    nlogn_fix_kernel<<<1024, 256, 0, st>>>(d_fix, g.F, fix);
+    const double fix = nlogn_fix_scale(g.F);  // per-bin rounding error 2^-(s+1)
+    if ((e = launch_nlogn_fix_table((unsigned long long *)d_fix, g.F, fix, st))) return e;
     const size_t smem = smem_bytes();
     if ((e = cudaFuncSetAttribute(onehot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
     if (p.n_tiles > 0)

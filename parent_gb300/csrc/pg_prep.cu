@@ -237,7 +237,19 @@ __global__ void nlogn_kernel(double *t, int nmax) {
         t[n] = n > 1 ? (double)n * log((double)n) : 0.0;
 }
 
+__global__ void nlogn_fix_kernel(unsigned long long *t, int nmax, double fix) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
+        t[n] = n > 1 ? (unsigned long long)llrint((double)n * log((double)n) * fix) : 0ull;
+}
+
 }  // namespace
+
+cudaError_t launch_nlogn_fix_table(unsigned long long *nfix, int nmax, double fix, cudaStream_t st) {
+    int blocks = (nmax + 1 + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    nlogn_fix_kernel<<<blocks, 256, 0, st>>>(nfix, nmax, fix);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st) {
     int blocks = (nmax + 1 + 255) / 256;
