@@ -65,7 +65,12 @@ def sizes(n_dih: int) -> dict:
 
 
 def _cols64(bonds, angles, dihedrals):
-    return [np.ascontiguousarray(a, dtype=np.float64).copy() for a in (bonds, angles, dihedrals)]
+    b, a, d = [np.ascontiguousarray(x, dtype=np.float64).copy() for x in (bonds, angles, dihedrals)]
+    nd = d.shape[0]
+    if b.ndim != 2 or a.ndim != 2 or d.ndim != 2 or b.shape[0] != nd + 2 or a.shape[0] != nd + 1 \
+            or not (b.shape[1] == a.shape[1] == d.shape[1]):
+        raise ValueError(f"need (nDih+2, F), (nDih+1, F), (nDih, F) columns, got {b.shape}, {a.shape}, {d.shape}")
+    return [b, a, d]
 
 
 def read_bat(path) -> tuple:

@@ -146,6 +146,7 @@ static DofArrays dof_arrays(pg_ctx *ctx, int D) {
     d.s1 = base + 3 * (size_t)D;
     d.acon = base + 4 * (size_t)D;
     d.b2 = (int *)(base + 5 * (size_t)D);
+    d.m2 = d.b2 + D;
     return d;
 }
 
@@ -215,7 +216,7 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     CK(cudaEventRecord(ctx->ev[1], st));
 
     CK(ctx->bins.ensure((size_t)D * g.ldb));
-    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + sizeof(int)) + 64));
+    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
     CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
     if (ctx->nlogn_max < g.F) {
@@ -776,7 +777,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         L.bins = off;
         off = al256(off + (size_t)g.D * g.ldb);
         L.dof = off;
-        off = al256(off + (size_t)g.D * (5 * sizeof(double) + sizeof(int)) + 64);
+        off = al256(off + (size_t)g.D * (5 * sizeof(double) + 2 * sizeof(int)) + 64);
         L.par = off;
         off = al256(off + (size_t)par_layout(g.n_dih).total * sizeof(double));
         L.mi = off;
@@ -811,6 +812,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         d.s1 = b + 3 * (size_t)D;
         d.acon = b + 4 * (size_t)D;
         d.b2 = (int *)(b + 5 * (size_t)D);
+        d.m2 = d.b2 + D;
         return d;
     };
     std::vector<SysDesc> sd((size_t)n_sys);

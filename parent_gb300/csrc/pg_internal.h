@@ -42,6 +42,7 @@ struct DofArrays {
     double *acon;            // ln(binsize_2D) + (1/N) sum_k m(k) ln J(k), the
                              // per-DOF constant of the 2D entropy decomposition
     int *b2;                 // 2D bin count of the DOF's type
+    int *m2;                 // largest marginal count over the DOF's 2D bins
 };
 
 // Offsets of the nine .par body blocks inside one contiguous double buffer.

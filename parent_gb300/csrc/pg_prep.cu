@@ -27,18 +27,54 @@ __device__ __forceinline__ double load_val(const void *col, int prec, int64_t f)
     return prec ? __ldg((const double *)col + f) : (double)__ldg((const float *)col + f);
 }
 
-// x + modFit - 2 pi int((x + modFit) / (2 pi)), PARENT.cpp:611, evaluated as
-// the reference's left-to-right expression without contraction.
+// q = int((x + modFit) / (2 pi)) and x + modFit - 2 pi q, PARENT.cpp:611,
+// evaluated as the reference's left-to-right expression without contraction.
+__device__ __forceinline__ int shift_quot(double t, double twopi) { return __double2int_rz(__ddiv_rn(t, twopi)); }
+__device__ __forceinline__ double shift_apply(double t, int q, double twopi) {
+    return __dsub_rn(t, __dmul_rn(twopi, (double)q));
+}
 __device__ __forceinline__ double shifted(double x, double modfit, double twopi) {
     const double t = __dadd_rn(x, modfit);
-    const int q = __double2int_rz(__ddiv_rn(t, twopi));
-    return __dsub_rn(t, __dmul_rn(twopi, (double)q));
+    return shift_apply(t, shift_quot(t, twopi), twopi);
 }
 
 __device__ __forceinline__ int bin_index(double x, double mn, double bs) {
     return __double2int_rz(__ddiv_rn(__dsub_rn(x, mn), bs));
 }
 
+// ---- FP32 screening of the FP64 bin decisions (FP32 input only).
+// Every decision above is int(q*) for a quotient q* = fl64(a / b) >= 0. The
+// screen forms q ~ q* in FP32 with a proven bound |q - q*| <= eps (from the
+// operands' magnitudes; every bound below carries a factor >= 4 of slack) and
+// accepts floor(q) only when no integer lies within eps of q; otherwise the
+// caller evaluates q* with the exact FP64 expression. The result is therefore
+// the reference's integer in every case; the FP64 pipe, a small fraction of
+// this part's FP32 rate, only sees the values that fall next to a boundary.
+
+// floor(q) if [q - eps, q + eps] (directed rounding) holds no integer and
+// q - eps >= 0, else -1 (also for NaN).
+__device__ __forceinline__ int screened_floor(float q, float eps) {
+    const float lo = __fsub_rd(q, eps), hi = __fadd_ru(q, eps);
+    const int il = __float2int_rd(lo), ih = __float2int_rd(hi);
+    return (lo >= 0.f && il == ih) ? il : -1;
+}
+
+// v ~ hi + lo as two floats (|v - hi - lo| <= 2^-48 |v|)
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 split2(double v) {
+    const float hi = __double2float_rn(v);
+    return {hi, __double2float_rn(__dsub_rn(v, (double)hi))};
+}
+
+// Extrema of a dihedral column after the shift: within one value of
+// q = int((x + modFit) / 2 pi) the shifted value is a non-decreasing function
+// of x (FP64 rounding is monotone), so the largest / smallest x of each q
+// region gives that region's extreme shifted value.
+constexpr int kRegions = 3;  // x in [0, 2 pi + 5e-9) and modFit in (0, 2 pi] give q in {0, 1, 2}
+
+template <bool F32>
 __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb,
                                                         const void *ca, const void *cd,
                                                         int64_t ld, int prec, DofArrays dof,
@@ -51,6 +87,7 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     const void *col = type == TB ? cb : (type == TA ? ca : cd);
     col = prec ? (const void *)((const double *)col + (int64_t)local * ld)
                : (const void *)((const float *)col + (int64_t)local * ld);
+    const float *colf = (const float *)col;
     const int F = geo.F;
     const int B1 = geo.bins[type], B2 = geo.bins[3 + type];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -62,14 +99,25 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     unsigned int *h2 = h1 + kWarps * B1;
     __shared__ double s_shift, s_mn, s_mx;
     __shared__ double red_mn[kWarps], red_mx[kWarps];
+    __shared__ float red_rmax[kWarps][kRegions], red_rmin[kWarps][kRegions];
 
     double modfit = 0.0;
     if (type == TD) {
         for (int k = tid; k < kWarps * kModfitBins; k += kThreads) hmod[k] = 0;
         __syncthreads();
         int bad = 0;
+        // x / modfit_bs: relative error of x32 * fl32(1/bs) <= 2^-23
+        const float rm = __double2float_rn(__drcp_rn(modfit_bs));
         for (int f = tid; f < F; f += kThreads) {
-            int idx = __double2int_rz(__ddiv_rn(load_val(col, prec, f), modfit_bs));
+            int idx = -1;
+            if (F32) {
+                const float x = __ldg(colf + f);
+                const float q = __fmul_rn(x, rm);
+                idx = screened_floor(q, __fmul_ru(q, 0x1p-21f));
+                if (idx < 0) idx = __double2int_rz(__ddiv_rn((double)x, modfit_bs));
+            } else {
+                idx = __double2int_rz(__ddiv_rn(load_val(col, prec, f), modfit_bs));
+            }
             if (idx < 0 || idx >= kModfitBins) { bad++; idx = idx < 0 ? 0 : kModfitBins - 1; }
             atomicAdd(&hmod[warp * kModfitBins + idx], 1u);
         }
@@ -112,25 +160,87 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
         modfit = s_shift;
     }
 
+    // FP32 images of the shift constants; t = x + modFit and its quotient by
+    // 2 pi are screened with |t32 - t| <= 2^-23 (|x| + |modFit|) <= 2e-6 and
+    // |q - t / 2 pi| <= 8e-7 for x < 2 pi + 5e-9, modFit <= 2 pi
+    const F2 mf2 = split2(modfit), tp2 = split2(twopi);
+    const float r2pi = __double2float_rn(__drcp_rn(twopi));
+    constexpr float kShiftEps = 4e-6f;
+    // exact quotient q of the shift for an FP32 value (screened, else FP64)
+    auto shift_q = [&](float x, float &t32) -> int {
+        t32 = __fadd_rn(__fadd_rn(x, mf2.hi), mf2.lo);
+        int q = screened_floor(__fmul_rn(t32, r2pi), kShiftEps);
+        if (q < 0) q = shift_quot(__dadd_rn((double)x, modfit), twopi);
+        return q;
+    };
+
     // ---- extrema (PARENT.cpp:512-521, 539-548, 614-623)
     double lmax = -1.0e100, lmin = 1.0e100;
-    for (int f = tid; f < F; f += kThreads) {
-        double x = load_val(col, prec, f);
-        if (type == TD) x = shifted(x, modfit, twopi);
-        if (x > lmax) lmax = x;
-        if (x < lmin) lmin = x;
+    if (F32) {
+        float rmax[kRegions], rmin[kRegions];
+        for (int r = 0; r < kRegions; r++) { rmax[r] = -INFINITY; rmin[r] = INFINITY; }
+        for (int f = tid; f < F; f += kThreads) {
+            const float x = __ldg(colf + f);
+            int r = 0;
+            if (type == TD) {
+                float t32;
+                r = shift_q(x, t32);
+                r = r < 0 ? 0 : (r >= kRegions ? kRegions - 1 : r);  // out of range: flagged above
+            }
+#pragma unroll
+            for (int k = 0; k < kRegions; k++) {
+                if (k == r) {
+                    rmax[k] = fmaxf(rmax[k], x);
+                    rmin[k] = fminf(rmin[k], x);
+                }
+            }
+        }
+        for (int k = 0; k < kRegions; k++) {
+            for (int o = 16; o > 0; o >>= 1) {
+                rmax[k] = fmaxf(rmax[k], __shfl_xor_sync(0xffffffffu, rmax[k], o));
+                rmin[k] = fminf(rmin[k], __shfl_xor_sync(0xffffffffu, rmin[k], o));
+            }
+            if (lane == 0) { red_rmax[warp][k] = rmax[k]; red_rmin[warp][k] = rmin[k]; }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int k = 0; k < kRegions; k++) {
+                float a = -INFINITY, b = INFINITY;
+                for (int w = 0; w < kWarps; w++) {
+                    a = fmaxf(a, red_rmax[w][k]);
+                    b = fminf(b, red_rmin[w][k]);
+                }
+                if (a < b) continue;  // empty region
+                double va = (double)a, vb = (double)b;
+                if (type == TD) {
+                    va = shifted(va, modfit, twopi);
+                    vb = shifted(vb, modfit, twopi);
+                }
+                if (va > lmax) lmax = va;
+                if (vb < lmin) lmin = vb;
+            }
+            red_mx[0] = lmax;
+            red_mn[0] = lmin;
+        }
+    } else {
+        for (int f = tid; f < F; f += kThreads) {
+            double x = load_val(col, prec, f);
+            if (type == TD) x = shifted(x, modfit, twopi);
+            if (x > lmax) lmax = x;
+            if (x < lmin) lmin = x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double a = __shfl_xor_sync(0xffffffffu, lmax, o);
+            const double b = __shfl_xor_sync(0xffffffffu, lmin, o);
+            if (a > lmax) lmax = a;
+            if (b < lmin) lmin = b;
+        }
+        if (lane == 0) { red_mx[warp] = lmax; red_mn[warp] = lmin; }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        const double a = __shfl_xor_sync(0xffffffffu, lmax, o);
-        const double b = __shfl_xor_sync(0xffffffffu, lmin, o);
-        if (a > lmax) lmax = a;
-        if (b < lmin) lmin = b;
-    }
-    if (lane == 0) { red_mx[warp] = lmax; red_mn[warp] = lmin; }
     __syncthreads();
     if (tid == 0) {
         double tmpMax = -1.0e100, tmpMin = 1.0e100;
-        for (int w = 0; w < kWarps; w++) {
+        for (int w = 0; w < (F32 ? 1 : kWarps); w++) {
             if (red_mx[w] > tmpMax) tmpMax = red_mx[w];
             if (red_mn[w] < tmpMin) tmpMin = red_mn[w];
         }
@@ -157,16 +267,58 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
     uint8_t *brow = bins + (int64_t)g * geo.ldb;
     int bad = 0;
-    for (int f = tid; f < F; f += kThreads) {
-        double x = load_val(col, prec, f);
-        if (type == TD) x = shifted(x, modfit, twopi);
-        int i1 = bin_index(x, mn, bs1);
-        int i2 = bin_index(x, mn, bs2);
-        if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
-        if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
-        atomicAdd(&h1[warp * B1 + i1], 1u);
-        atomicAdd(&h2[warp * B2 + i2], 1u);
-        brow[f] = (uint8_t)i2;
+    if (F32) {
+        // d = fl64(x' - mn) (x' the shifted value for dihedrals) is formed in
+        // FP32 from split constants, |d32 - d| <= 2^-20 E with
+        // E = |mn| + |mx| (+ 2|modFit| + 8 pi for dihedrals), a bound >= 4x
+        // the accumulated rounding; q_k = d32 * fl32(1 / bs_k) then has
+        // |q_k - q*| <= 2^-20 E / bs_k + 2^-22 q_k.
+        const F2 mn2 = split2(mn);
+        const float r1 = __double2float_rn(__drcp_rn(bs1)), r2 = __double2float_rn(__drcp_rn(bs2));
+        double E = fabs(mn) + fabs(mx);
+        if (type == TD) E = E + 2.0 * fabs(modfit) + 4.0 * twopi;
+        const float e1 = __double2float_ru(E * 0x1p-20 / bs1), e2 = __double2float_ru(E * 0x1p-20 / bs2);
+        for (int f = tid; f < F; f += kThreads) {
+            const float x = __ldg(colf + f);
+            float d32;
+            int q = 0;
+            if (type == TD) {
+                float t32;
+                q = shift_q(x, t32);
+                const float qf = (float)q;
+                d32 = __fsub_rn(__fsub_rn(__fsub_rn(__fsub_rn(t32, __fmul_rn(qf, tp2.hi)), __fmul_rn(qf, tp2.lo)),
+                                          mn2.hi),
+                                mn2.lo);
+            } else {
+                d32 = __fsub_rn(__fsub_rn(x, mn2.hi), mn2.lo);
+            }
+            const float q1 = __fmul_rn(d32, r1), q2 = __fmul_rn(d32, r2);
+            int i1 = screened_floor(q1, __fadd_ru(e1, __fmul_ru(fabsf(q1), 0x1p-21f)));
+            int i2 = screened_floor(q2, __fadd_ru(e2, __fmul_ru(fabsf(q2), 0x1p-21f)));
+            if (i1 < 0 || i2 < 0) {
+                double xv = (double)x;
+                if (type == TD) xv = shift_apply(__dadd_rn(xv, modfit), q, twopi);
+                if (i1 < 0) i1 = bin_index(xv, mn, bs1);
+                if (i2 < 0) i2 = bin_index(xv, mn, bs2);
+            }
+            if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
+            if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
+            atomicAdd(&h1[warp * B1 + i1], 1u);
+            atomicAdd(&h2[warp * B2 + i2], 1u);
+            brow[f] = (uint8_t)i2;
+        }
+    } else {
+        for (int f = tid; f < F; f += kThreads) {
+            double x = load_val(col, prec, f);
+            if (type == TD) x = shifted(x, modfit, twopi);
+            int i1 = bin_index(x, mn, bs1);
+            int i2 = bin_index(x, mn, bs2);
+            if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
+            if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
+            atomicAdd(&h1[warp * B1 + i1], 1u);
+            atomicAdd(&h2[warp * B2 + i2], 1u);
+            brow[f] = (uint8_t)i2;
+        }
     }
     if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);
     __syncthreads();
@@ -180,6 +332,12 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     __syncthreads();
 
     if (tid == 0) {
+        // largest 2D-bin marginal count: no 2D bin of a pair with this DOF
+        // can hold more frames
+        unsigned int m2 = 0;
+        for (int k = 0; k < B2; k++) m2 = h2[k] > m2 ? h2[k] : m2;
+        dof.m2[g] = (int)m2;
+
         // 1D entropy in the reference's order (PARENT.cpp:658-670, 702-714, 746-756)
         const int N = F;
         int occupbins = 0;
@@ -272,11 +430,10 @@ cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld,
     const double pi = acos(-1.0);  // PARENT.cpp:112
     const double modfit_bs = (2 * pi + 0.000000005) / kModfitBins;  // PARENT.cpp:569
     const size_t smem = prep_smem_bytes(g);
-    cudaError_t e = cudaFuncSetAttribute(prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    auto kern = double_prec ? prep_kernel<false> : prep_kernel<true>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    prep_kernel<<<g.D, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof,
-                                             bins, err, modfit_bs, pi);
+    kern<<<g.D, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof, bins, err, modfit_bs, pi);
     return cudaGetLastError();
 }
 

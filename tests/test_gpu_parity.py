@@ -344,3 +344,85 @@ def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
     want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, bins, pairs)
     for p, x, y in zip(pairs, got, want):
         assert np.array_equal(x, y), p
+
+
+def _boundary_column(rng, lo, hi, Bs, F, pad=5e-9):
+    """FP32 column on [lo, hi] (both present) packed with the float values
+    next to every bin edge mn + k*bs (mn = lo - pad, mx = hi + pad) of each
+    bin count in Bs: the values whose bin the FP32 screen cannot decide."""
+    lo, hi = np.float32(lo), np.float32(hi)
+    mn, mx = np.float64(lo) - pad, np.float64(hi) + pad
+    vals = [lo, hi]
+    for B in Bs:
+        bs = (mx - mn) / B
+        for k in range(1, B):
+            e = np.float32(mn + k * bs)
+            vals += [np.nextafter(e, np.float32(-1e9)), e, np.nextafter(e, np.float32(1e9))]
+    vals = np.array([v for v in vals if lo <= v <= hi], dtype=np.float32)
+    fill = rng.uniform(float(lo), float(hi), F - vals.size).astype(np.float32)
+    col = np.concatenate([vals, fill])
+    rng.shuffle(col)
+    return col
+
+
+def _dihedral_boundaries(rng, col, B, target_mn, target_mx, shift):
+    """Adds to a dihedral column the float x whose shifted value lies next to
+    a bin edge of the shifted range (extrema and shift taken from the oracle
+    on the column without them) and next to the shift's own 2 pi edge."""
+    twopi = 2 * np.pi
+    out = []
+    for k in range(1, B):
+        t = target_mn + k * (target_mx - target_mn) / B
+        x = t - shift
+        if x < 0:
+            x += twopi
+        e = np.float32(x)
+        out += [np.nextafter(e, np.float32(-1)), e, np.nextafter(e, np.float32(10))]
+    e = np.float32(twopi - shift)
+    out += [np.nextafter(e, np.float32(-1)), e, np.nextafter(e, np.float32(10))]
+    return np.array(out, dtype=np.float32)
+
+
+def test_fp32_bin_edges_bit_exact(eng):
+    """FP32 values adjacent to every 1D and 2D bin edge (and the dihedral
+    shift's 2 pi edge) get the reference's bins: pair counts, per-DOF
+    extrema/shift and 1D entropies agree with the FP64 oracle."""
+    rng = np.random.default_rng(2024)
+    n_dih, F = 3, 30000
+    B1, B2 = 37, 50
+    bins = (B1, B1, B1, B2, B2, B2)
+    bonds = np.stack([_boundary_column(rng, 0.14 + 0.01 * k, 0.17 + 0.013 * k, (B1, B2), F) for k in range(n_dih + 2)])
+    angles = np.stack([_boundary_column(rng, 1.2 + 0.1 * k, 2.4 + 0.05 * k, (B1, B2), F) for k in range(n_dih + 1)])
+    # dihedral 0: a gap at 2 pi (longest empty run); 1: fully occupied (first
+    # minimum bin); 2: concentrated near pi
+    base = [rng.uniform(0.5, 5.0, F).astype(np.float32),
+            rng.uniform(0.0, 2 * np.pi - 1e-3, F).astype(np.float32),
+            np.mod(rng.normal(np.pi, 0.4, F), 2 * np.pi).astype(np.float32)]
+    dih = []
+    for k, col in enumerate(base):
+        tb = np.zeros((3, F), np.float32) + 0.15
+        ta = np.zeros((2, F), np.float32) + 1.5
+        mn, mx, sh, _, bad = oracle.extrema(tb, ta, col[None, :])
+        assert bad == 0
+        extra = np.concatenate([_dihedral_boundaries(rng, col, B, mn[-1], mx[-1], sh[-1]) for B in (B1, B2)])
+        extra = extra[(extra >= col.min()) & (extra <= col.max())]
+        c = col.copy()
+        c[rng.choice(F, extra.size, replace=False)] = extra
+        dih.append(c)
+    dih = np.stack(dih)
+    traj = pg.Trajectory(np.ascontiguousarray(bonds), np.ascontiguousarray(angles), np.ascontiguousarray(dih))
+    D = 3 * n_dih + 3
+    pairs = [(i, j) for i in range(D) for j in range(i + 1, D)]
+    got = eng.pair_counts(traj, bins, pairs)
+    want = oracle.pair_counts(bonds, angles, dih, bins, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
+    mn, mx, sh = eng.dof_stats(D)
+    omn, omx, osh, _, bad = oracle.extrema(bonds, angles, dih)
+    assert bad == 0
+    assert np.array_equal(mn.view(np.uint64), omn.view(np.uint64))
+    assert np.array_equal(mx.view(np.uint64), omx.view(np.uint64))
+    assert np.array_equal(sh.view(np.uint64), osh.view(np.uint64))
+    body = eng.entropy(traj, bins, "hist")
+    ref = oracle.parent(bonds, angles, dih, bins)
+    compare_bodies(n_dih, body, ref)
