@@ -56,6 +56,15 @@ METRIC = "DOF-pair x frame updates/s @50 bins (all-pairs 2D-histogram MI + MIST)
 UNIT = "updates/s"
 
 
+def hist_slots(bins: int) -> int:
+    """Pair slots per CTA of the histogram layout the library picks (32 with
+    32-bit counters up to 35 bins, else 16; PG_HIST_SLOTS forces one)."""
+    forced = os.environ.get("PG_HIST_SLOTS")
+    if forced in ("16", "32"):
+        return 32 if forced == "32" and bins <= 50 else 16
+    return 32 if bins <= 35 else 16
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,6 +344,7 @@ def run_batch(args):
             "config": {"workload": BATCH, "systems": len(systems), "dofs": [min(Ds), max(Ds)],
                        "frames": [min(Fs), max(Fs)], "updates_per_step": units, "input": "fp32",
                        "bins": args.bins, "form": "hist",
+                       "hist_slots": hist_slots(args.bins),
                        "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (total_bytes / 1e9)},
             "sequential": {"ms_per_step": ms_seq, "value": units * world / (ms_seq / 1e3),
@@ -446,9 +456,17 @@ def run_gb300(args):
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
+        parts = []
         for _ in range(args.e2e_steps):
+            w0 = time.perf_counter()
             eng.entropy(hview, bins, args.form, out=body)
+            te = eng.timings()
+            w1 = time.perf_counter()
             edges, totals = eng.mist(n_dih)
+            tm = eng.timings()
+            parts.append({"entropy_wall_ms": (w1 - w0) * 1e3, "mist_wall_ms": (time.perf_counter() - w1) * 1e3,
+                          "transfer_ms": float(te[3]), "prep_ms": float(te[0]), "pairs_ms": float(te[1]),
+                          "entropy_device_ms": float(te[4]), "mist_ms": float(tm[2])})
         t1 = time.perf_counter()
         sec = (t1 - t0) / args.e2e_steps
         if dist:
@@ -456,7 +474,8 @@ def run_gb300(args):
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             sec = float(tt.item())
         e2e = {"value": units * world / sec, "unit": UNIT, "h2d_bytes_per_step": D * F * es,
-               "d2h_bytes_per_step": total * 8 + (D - 1) * (4 * 4 + 8 + 8), "ms_per_step": sec * 1e3}
+               "d2h_bytes_per_step": total * 8 + (D - 1) * (4 * 4 + 8 + 8), "ms_per_step": sec * 1e3,
+               "breakdown": parts[-1]}
         pg._check(pg.lib().pg_host_free_pinned(host))
         pg._check(pg.lib().pg_host_free_pinned(hout))
 
@@ -499,6 +518,7 @@ def run_gb300(args):
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": args.workload, "n_atoms": n_atoms, "dofs": D, "pairs": P, "frames": F,
                        "input": "fp64" if prec else "fp32", "bins": args.bins, "form": form,
+                       "hist_slots": hist_slots(args.bins) if form == "hist" else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (D * F * es / 1e9)},
             "kernel_ms": {"prep": statistics.mean(prep_ms), "pairs": statistics.mean(pair_ms),

@@ -177,7 +177,7 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     g.nd = g.n_dih;
     g.D = g.nb + g.na + g.nd;
     g.F = tv->n_frames;
-    g.ldb = ((int64_t)g.F + 4095) / 4096 * 4096;
+    g.ldb = bins_ld(g.F);
     for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
     ctx->resident = false;
     const int D = g.D;
@@ -233,19 +233,6 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     return PG_OK;
 }
 
-// Fixed-point n ln n table covering counts up to F. A table built for a
-// larger F is reused: its scale is no larger, so sums still fit 64 bits.
-static int ensure_fix_table(pg_ctx *ctx, int F) {
-    if (ctx->nfix_max >= F) return PG_OK;
-    const double fix = nlogn_fix_scale(F);
-    CK(ctx->nfix.ensure(((size_t)F + 1) * sizeof(unsigned long long)));
-    CK(launch_nlogn_fix_table((unsigned long long *)ctx->nfix.p, F, fix, ctx->stream));
-    ctx->launches++;
-    ctx->nfix_max = F;
-    ctx->nfix_scale = fix;
-    return PG_OK;
-}
-
 static int check_err_words(pg_ctx *ctx) {
     int h[ERR_WORDS];
     CK(cudaMemcpyAsync(h, ctx->errw.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
@@ -262,14 +249,29 @@ static int bmax_of(const SysGeom &g) {
     return std::max(g.bins[3], std::max(g.bins[4], g.bins[5]));
 }
 
-// Histogram layout: the 16-slot kernel (32-bit counters, two frame
-// sub-streams per pair) is the default; it measured 3.47 s against 5.40 s for
-// the 32-slot kernel (16-bit conflict-free counters with windowed folding) at
-// 7,494 DOFs x 500,000 frames x 50 bins. PG_HIST_SLOTS=32 selects the latter
-// (2D bins <= 50).
+// Fixed-point n ln n table covering counts up to F. A table built for a
+// larger F is reused: its scale is no larger, so sums still fit 64 bits.
+static int ensure_fix_table(pg_ctx *ctx, int F) {
+    if (ctx->nfix_max >= F) return PG_OK;
+    const double fix = nlogn_fix_scale(F);
+    CK(ctx->nfix.ensure(((size_t)F + 1) * sizeof(unsigned long long)));
+    CK(launch_nlogn_fix_table((unsigned long long *)ctx->nfix.p, F, fix, ctx->stream));
+    ctx->launches++;
+    ctx->nfix_max = F;
+    ctx->nfix_scale = fix;
+    return PG_OK;
+}
+
+// Histogram layout, from measured inner-loop rates: the 32-slot kernel with
+// 32-bit counters (one wavefront per warp-wide reduction) for 2D bin counts
+// up to 35; the 16-slot kernel (two lanes per pair) above that, where the
+// 32-slot kernel needs 16-bit counters and runs slower. PG_HIST_SLOTS=16 or
+// 32 forces one layout (32 slots up to 50 bins).
 static bool use_hist32(const SysGeom &g) {
     const char *e = getenv("PG_HIST_SLOTS");
-    return e && atoi(e) == 32 && pairs_hist32_supported(bmax_of(g));
+    if (e && atoi(e) == 16) return false;
+    if (e && atoi(e) == 32) return pairs_hist32_supported(bmax_of(g));
+    return pairs_hist32_wide(bmax_of(g));
 }
 
 // Launches the 32-slot kernel over the cached full tile list (explicit ==
@@ -299,13 +301,12 @@ static int run_hist32(pg_ctx *ctx, const SysGeom &g, const DofArrays &dof, const
         tiles = (const PairTile *)ctx->tiles.p;
         n = (int64_t)ctx->tiles_host.size();
     }
-    int n_sm = 0;
-    CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(n, n_sm));
-    const size_t sb = pairs_hist32_scratch_bytes(bmax_of(g), grid);
+    const size_t sb = pairs_hist32_scratch_bytes(bmax_of(g), pairs_hist32_grid(n));
     CK(ctx->scratch.ensure(sb));
-    CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const double *)ctx->nlogn.p, tiles, n, grid, po,
-                           (int *)ctx->errw.p, ctx->scratch.p, sb, st));
+    int rc = ensure_fix_table(ctx, g.F);
+    if (rc) return rc;
+    CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                           ctx->nfix_scale, tiles, n, po, (int *)ctx->errw.p, ctx->scratch.p, sb, st));
     ctx->launches++;
     if (explicit_tiles) {
         CK(cudaStreamSynchronize(st));  // the private tile buffer is released on return
@@ -765,7 +766,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         g.nd = g.n_dih;
         g.D = g.nb + g.na + g.nd;
         g.F = v.n_frames;
-        g.ldb = ((int64_t)g.F + 4095) / 4096 * 4096;
+        g.ldb = bins_ld(g.F);
         for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
         L.prec = v.double_prec;
         L.own_cols = !v.on_device;
@@ -798,6 +799,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     }
     char *arena = (char *)ctx->batch.p;
     const int bmax = bmax_of(sys[0].g);
+    const bool h32 = use_hist32(sys[0].g);
     int T = 0, fc = 0, nst = 0;
     if (!pairs_hist_config(bmax, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
 
@@ -845,7 +847,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     for (int s = 0; s < n_sys; s++) order[s] = s;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a].g.F > sys[b].g.F; });
     for (int s : order) {
-        std::vector<PairTile> t = build_tiles(sys[s].g.D, T);
+        std::vector<PairTile> t = h32 ? build_tiles32(sys[s].g.D) : build_tiles(sys[s].g.D, T);
         tiles.insert(tiles.end(), t.begin(), t.end());
         tsys.insert(tsys.end(), t.size(), s);
     }
@@ -859,7 +861,13 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     // recaptured when any of them change
     std::vector<int64_t> key = {(int64_t)n_sys, (int64_t)(uintptr_t)arena, (int64_t)(uintptr_t)meta,
                                 (int64_t)(uintptr_t)ctx->nfix.p, (int64_t)(uintptr_t)ctx->errw.p};
+    size_t sb32 = 0;
+    if (h32) {
+        sb32 = pairs_hist32_scratch_bytes(bmax, pairs_hist32_grid((int64_t)tiles.size()));
+        CK(ctx->scratch.ensure(sb32));
+    }
     key.push_back((int64_t)ctx->nfix_max);
+    key.push_back(h32 ? (int64_t)(uintptr_t)ctx->scratch.p : -1);
     for (int k = 0; k < 6; k++) key.push_back(bins[k]);
     for (int s = 0; s < n_sys; s++) {
         const pg_bat_view &v = trajs[s];
@@ -924,10 +932,14 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
                 e = cudaMemcpyAsync(arena + L.par, d.s1, (size_t)L.g.D * sizeof(double), cudaMemcpyDeviceToDevice, st);
         }
         if (e == cudaSuccess)
-            e = launch_pairs_hist_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
-                                        (const int *)(meta + mo_ts), (int64_t)tiles.size(),
-                                        (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,
-                                        (int *)ctx->errw.p, T, st);
+            e = h32 ? launch_pairs_hist32_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
+                                                (const int *)(meta + mo_ts), (int64_t)tiles.size(),
+                                                (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,
+                                                (int *)ctx->errw.p, ctx->scratch.p, sb32, st)
+                    : launch_pairs_hist_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
+                                              (const int *)(meta + mo_ts), (int64_t)tiles.size(),
+                                              (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,
+                                              (int *)ctx->errw.p, T, st);
         if (e == cudaSuccess) e = launch_mist_batch((const MistDesc *)(meta + mo_md), n_sys, maxD, st);
         cudaError_t e2 = cudaStreamEndCapture(st, &graph);
         if (e == cudaSuccess) e = e2;

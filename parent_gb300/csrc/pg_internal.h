@@ -26,7 +26,7 @@ enum {
 struct SysGeom {
     int n_dih, nb, na, nd, D;  // D = nb + na + nd
     int F;                     // frames
-    int64_t ldb;               // bytes between DOF rows of the uint8 bin matrix
+    int64_t ldb;               // bytes between DOF rows of the uint8 bin matrix (bins_ld(F))
     int bins[6];               // b1D a1D d1D b2D a2D d2D
 };
 
@@ -108,6 +108,11 @@ struct SysDesc {
     double lnN;
 };
 
+// Row pitch of the uint8 bin matrix: a multiple of 4096 with at least 4096
+// bytes past the last frame, so a pair kernel's last chunk (any chunk size up
+// to 4096 frames) stays inside its row.
+inline int64_t bins_ld(int F) { return ((int64_t)F + 4095) / 4096 * 4096 + 4096; }
+
 // 2^s with s as large as possible (<= 44) such that F ln F * 2^s stays below
 // 1.6e19: sums of n ln n over a histogram of F frames, rounded to multiples
 // of 2^-s, then fit in 64-bit unsigned integers.
@@ -129,13 +134,20 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
 int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages);
 
 // 32-slot histogram pair kernel (2D bins <= 50): 16-bit conflict-free
-// counters folded into a per-CTA 32-bit accumulator (scratch) every 63,488
-// frames; persistent grid of `grid` CTAs over 4 x 8-DOF tiles.
+// counters over 4 x 8-DOF tiles, persistent grid of pairs_hist32_grid(n)
+// CTAs; tiles that could overflow a 16-bit counter move counts into a per-CTA
+// overflow area in `scratch` (pairs_hist32_scratch_bytes, zeroed by the
+// launcher) every 32,768 frames.
 bool pairs_hist32_supported(int bmax);
+bool pairs_hist32_wide(int bmax);  // 32-bit counters fit (2D bins <= 35)
+int pairs_hist32_grid(int64_t n_tiles);
 size_t pairs_hist32_scratch_bytes(int bmax, int grid);
-cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, const double *nlogn,
-                                const PairTile *tiles, int64_t n_tiles, int grid, PairOut out, int *err,
-                                void *scratch, size_t scratch_bytes, cudaStream_t st);
+cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                                const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
+                                PairOut out, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
+cudaError_t launch_pairs_hist32_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
+                                      int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
+                                      void *scratch, size_t scratch_bytes, cudaStream_t st);
 
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,

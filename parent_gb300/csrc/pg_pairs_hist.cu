@@ -7,12 +7,12 @@
 // tile list with a stride of the grid size, so the CTA's shared-memory
 // histograms, barriers and staging ring live across tiles.
 //
-// Warp 31 is the producer: one lane streams every chunk of every tile of the
-// CTA, the tile's 2T uint8 bin rows per chunk, into a ring of shared-memory
-// stages with bulk TMA copies (cp.async.bulk, completion on a full[] mbarrier)
-// and refills a stage once every consumer warp has released it (empty[]). It
-// runs ahead into the next tile while the consumers finish the current one,
-// so no tile starts with an empty pipeline.
+// Warp 31 is the producer: it streams every chunk of every tile of the CTA,
+// the tile's 2T uint8 bin rows per chunk, into a ring of shared-memory stages
+// with bulk TMA copies (cp.async.bulk, completion on a full[] mbarrier), one
+// row per lane issued in parallel, and refills a stage once every consumer
+// warp has released it (empty[]). It runs ahead into the next tile while the
+// consumers finish the current one, so no tile starts with an empty pipeline.
 //
 // Warps 0-30 consume: every lane owns one pair slot p and a frame sub-stream
 // and adds 1 to hist[(br*Bc + bc)*PPS + p] with a shared-memory reduction, so
@@ -132,47 +132,49 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist_kernel(const __grid_co
 
     if (warp == kConsumers) {
         // ---------------------------------------------------------- producer
-        if (lane == 0) {
-            long long seq = 0;
-            bool ok = true;
-            for (int64_t t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
-                const SysDesc &d = sys_of(t);
-                const PairTile tile = a.tiles[t];
-                const int nchunks = (d.geo.F + fc - 1) / fc;
-                const uint8_t *src[NROW];
-                uint32_t bytes = 0;
-                for (int k = 0; k < NROW; k++) {
-                    const int g = k < T ? (k < tile.nrow ? tile.row0 + k : -1)
-                                        : ((k - T) < tile.ncol ? tile.col0 + (k - T) : -1);
-                    src[k] = g >= 0 ? d.bins + (int64_t)g * d.geo.ldb : nullptr;
-                    bytes += g >= 0 ? (uint32_t)fc : 0u;
-                }
-                for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
-                    const int st = (int)(seq % nst);
+        // lane 0 waits for a free stage and arms its full barrier; lanes
+        // 0..NROW-1 then issue one row copy each, in parallel
+        long long seq = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
+            const SysDesc &d = sys_of(t);
+            const PairTile tile = a.tiles[t];
+            const int nchunks = (d.geo.F + fc - 1) / fc;
+            const uint8_t *src = nullptr;
+            if (lane < NROW) {
+                const int k = lane;
+                const int g = k < T ? (k < tile.nrow ? tile.row0 + k : -1)
+                                    : ((k - T) < tile.ncol ? tile.col0 + (k - T) : -1);
+                src = g >= 0 ? d.bins + (int64_t)g * d.geo.ldb : nullptr;
+            }
+            const uint32_t bytes = (uint32_t)__popc(__ballot_sync(0xffffffffu, src != nullptr)) * (uint32_t)fc;
+            for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
+                const int st = (int)(seq % nst);
+                int go = 1;
+                if (lane == 0) {
                     if (seq >= nst &&
                         !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((seq / nst) - 1) & 1))) {
                         s_pabort = 1;
-                        ok = false;
-                        break;
+                        go = 0;
+                    } else if (s_abort) {  // the consumers gave up: stop issuing
+                        go = 0;
                     }
-                    if (s_abort) {  // the consumers gave up: stop issuing
-                        ok = false;
-                        break;
-                    }
-                    // generic-proxy reads of this stage (released by the
-                    // empty barrier) before the async-proxy writes refilling it
+                    if (go) mbar_expect_tx(smem_u32(&full[st]), bytes);
+                }
+                if (!__shfl_sync(0xffffffffu, go, 0)) {
+                    ok = false;
+                    break;
+                }
+                if (src) {
+                    // generic-proxy reads of this stage (released by the empty
+                    // barrier) before the async-proxy writes refilling it
                     fence_proxy_async();
-                    const uint32_t bar = smem_u32(&full[st]);
-                    mbar_expect_tx(bar, bytes);
-                    for (int k = 0; k < NROW; k++) {
-                        if (!src[k]) continue;
-                        bulk_g2s(smem_u32(stage + (size_t)(st * NROW + k) * fcs), src[k] + (int64_t)chunk * fc,
-                                 (uint32_t)fc, bar);
-                    }
+                    bulk_g2s(smem_u32(stage + (size_t)(st * NROW + lane) * fcs), src + (int64_t)chunk * fc,
+                             (uint32_t)fc, smem_u32(&full[st]));
                 }
             }
-            s_issued = seq;
         }
+        if (lane == 0) s_issued = seq;
     } else {
         // --------------------------------------------------------- consumers
         const int p = lane % PPS, sub = lane / PPS;
@@ -216,16 +218,22 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist_kernel(const __grid_co
                             // two frames per 32-bit IMAD: bytes spread into
                             // 16-bit halves, idx = br*Bc + bc < 65536 never
                             // carries across
+                            uint32_t ix[8];
 #pragma unroll
                             for (int q = 0; q < 4; q++) {
-                                const uint32_t i01 =
-                                    __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
-                                const uint32_t i23 =
-                                    __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
-                                red_add1_at(hbase + ((i01 & 0xffffu) << SH));
-                                red_add1_at(hbase + ((i01 >> 16) << SH));
-                                red_add1_at(hbase + ((i23 & 0xffffu) << SH));
-                                red_add1_at(hbase + ((i23 >> 16) << SH));
+                                ix[2 * q] = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
+                                ix[2 * q + 1] = __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
+                            }
+                            // frames in the order 0, 4, 8, 12, 1, 5, ...: consecutive
+                            // reductions of a lane are four frames apart (runs of one
+                            // bin do not queue back-to-back read-modify-writes on one word)
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+#pragma unroll
+                                for (int q = 0; q < 4; q++) {
+                                    const uint32_t v = ix[2 * q + (k >> 1)];
+                                    red_add1_at(hbase + (((k & 1) ? (v >> 16) : (v & 0xffffu)) << SH));
+                                }
                             }
                         } else {  // ragged end of the trajectory
                             const int n = fvalid - off;
@@ -381,6 +389,9 @@ __global__ void __launch_bounds__(1024) smem_red_probe(int iters, unsigned int *
 // the largest 2D bin count. PG_HIST_FC / PG_HIST_STAGES override the staging
 // for tuning sweeps when they fit.
 int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages) {
+    // the largest chunks that fit: measured rates fall with the chunk size
+    // (per-chunk synchronisation), and a chunk size that splits evenly over
+    // the 62 (warp, sub-stream) slots (3,968) measured no better than 4,096
     static const int cand[][2] = {{4096, 2}, {2048, 4}, {2048, 3}, {2048, 2}, {1024, 4}, {1024, 2}};
     int ofc = 0, onst = 0;
     if (const char *e = getenv("PG_HIST_FC")) ofc = atoi(e);
@@ -390,9 +401,8 @@ int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages) {
             return T == 4 ? smem_bytes<4>(bmax, fc, nst)
                           : (T == 2 ? smem_bytes<2>(bmax, fc, nst) : smem_bytes<1>(bmax, fc, nst));
         };
-        // chunk sizes divide 4096, the padding of every bin row, so the last
-        // chunk never reads past its row
-        const bool ovr = ofc >= 512 && ofc <= 4096 && 4096 % ofc == 0 && onst >= 2 && onst <= kMaxStages;
+        // a chunk of at most 4096 frames never reads past its row (bins_ld)
+        const bool ovr = ofc >= 256 && ofc <= 4096 && ofc % 16 == 0 && onst >= 2 && onst <= kMaxStages;
         if (ovr && need(ofc, onst) + 1024 <= (size_t)kSmemMax) {
             *tile_dim = T; *chunk_frames = ofc; *stages = onst;
             return (int)need(ofc, onst);

@@ -1,23 +1,39 @@
 // Pair kernel, shared-memory histogram form with 32 conflict-free pair slots
 // (2D bin counts up to 50).
 //
-// Same work as pairs_hist_kernel (the 2D fill + epilogue loops of
+// Same work as the 16-slot kernel (the 2D fill + epilogue loops of
 // PARENT.cpp :786-1479): per pair, the B1 x B2 histogram of (bin_i, bin_j)
 // over all frames, reduced to sum n ln n and the occupied-bin count, then
-// S2D and MI. The difference is the shared-memory layout:
-//   - a tile is 4 row DOFs x 8 column DOFs = 32 pair slots, lane = slot, and
-//     every lane of a warp counts the same 16 frames for its own pair;
-//   - counters are 16-bit, two bins per word: word (b >> 1) * 32 + lane, half
-//     b & 1, so lane l always hits bank l: one wavefront per warp-wide
-//     reduction instead of two;
-//   - a 16-bit counter holds at most 65,535, so every kWindowChunks chunks
-//     (63,488 frames) the consumer warps fold the halves into a per-CTA
-//     32-bit accumulator in global memory (L2-resident) and clear them.
-// The grid is persistent (one CTA per SM, tiles strided by the grid size) so
-// each CTA owns one accumulator slot. Staging is the warp-specialised
-// TMA/mbarrier pipeline of the 16-slot kernel: one producer warp issues
-// cp.async.bulk copies of the tile's 12 bin rows, 31 consumer warps count.
+// S2D and MI. The difference is the shared-memory layout: a tile is 4 row
+// DOFs x 8 column DOFs = 32 pair slots, lane = slot, every lane of a warp
+// counts the same 16 frames for its own pair, and lane l's counters all sit
+// in bank l, so a warp-wide reduction is one wavefront where the 16-slot
+// layout (two lanes per pair) needs two. The counters are
+//   - 32-bit, word b * 32 + lane, for 2D bin counts up to 35 (157 KB): the
+//     fastest layout there (17.2 updates/clock/SM in the inner loop alone,
+//     against 12.3 for the 16-slot layout);
+//   - 16-bit, two bins per word: word (b >> 1) * 32 + lane, half b & 1, for
+//     36 to 50 bins. Choosing the half costs instructions on every update and
+//     the loop ran at 10.8 updates/clock/SM, below the 16-slot layout, so this
+//     variant is only used on request.
+//
+// A 16-bit counter holds 65,535. No 2D bin of a pair can hold more frames
+// than the smaller of its two DOFs' largest marginal bin counts (computed by
+// the preprocessing kernel), so a tile whose pairs all stay within 65,535 by
+// that bound runs without any check. Other tiles (long trajectories with
+// peaked distributions) stop every 32,768 frames: the consumer warps move
+// 32,768 out of every counter that reached it into a per-CTA overflow count
+// in global memory (rare, L2-resident), so no counter can pass 65,535 within
+// the next 32,768 frames; the epilogue adds those counts back.
+//
+// Persistent grid (one CTA per SM, tiles strided by the grid size), with the
+// warp-specialised TMA/mbarrier pipeline of the 16-slot kernel: the producer
+// warp streams every chunk of every tile of the CTA (12 bin rows per chunk,
+// one row copy per lane) and runs ahead into the next tile; 31 consumer warps
+// count. The epilogue
+// (fixed-point n ln n table, integer atomics) matches the 16-slot kernel's.
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -32,236 +48,393 @@ namespace {
 using namespace dev;
 
 constexpr int kThreads = 1024, kWarps = 32, kConsumers = kWarps - 1;
+constexpr int kConsumerThreads = kConsumers * 32;
 constexpr int kRows = 4, kCols = 8;        // tile: 4 row DOFs x 8 column DOFs
 constexpr int kNRow = kRows + kCols;       // staged bin rows per chunk
-constexpr int kFC = 2048;                  // frames per chunk
-constexpr int kStages = 2;
+constexpr int kMaxStages = 6;
 constexpr int kPad = 32;                   // bytes between staged rows
-constexpr int kFCS = kFC + kPad;
-constexpr int kWindowChunks = 31;          // 31 x 2048 = 63,488 <= 65,535 counts per 16-bit half
-constexpr int kBmax = 50;                  // 32 lanes x 1,250 words x 4 B = 160 KB of counters
+constexpr int kFoldFrames = 32768;         // counts moved out per fold; frames between folds
+constexpr int kBmax16 = 50;                // 16-bit: 32 lanes x 1,250 words x 4 B = 160 KB of counters
+constexpr int kBmax32 = 35;                // 32-bit: 32 lanes x 1,225 words x 4 B = 157 KB
 constexpr int kSmemMax = 232448;
 
-__host__ __device__ constexpr int words_per_lane(int bmax) { return (bmax * bmax + 1) / 2; }
-__host__ __device__ constexpr size_t hist32_bytes(int bmax) {
-    return ((size_t)words_per_lane(bmax) * 32 * 4 + 1023) / 1024 * 1024;
+// 32-bit counters (one bin per word) where they fit, else 16-bit halves
+__host__ __device__ constexpr bool wide_counters(int bmax) { return bmax <= kBmax32; }
+__host__ __device__ constexpr int words_per_lane(int bmax) {
+    return wide_counters(bmax) ? bmax * bmax : (bmax * bmax + 1) / 2;
 }
-constexpr size_t kStageBytes = (size_t)kStages * kNRow * kFCS;
-constexpr size_t kRedBytes = (size_t)kWarps * 32 * (8 + 4);  // epilogue partials
+__host__ __device__ constexpr size_t hist32_bytes(int bmax) {
+    return ((size_t)words_per_lane(bmax) * 32 * 4 + 127) / 128 * 128;
+}
+size_t smem_bytes(int bmax, int fc, int nst) {
+    return hist32_bytes(bmax) + (size_t)nst * kNRow * (fc + kPad) + 8 * 2 * kMaxStages;
+}
 
-__global__ void __launch_bounds__(kThreads, 1)
-pairs_hist32_kernel(SysGeom geo, const uint8_t *__restrict__ bins, DofArrays dof,
-                    const double *__restrict__ nlogn, const PairTile *__restrict__ tiles, int n_tiles,
-                    PairOut out, int *err, uint32_t *__restrict__ acc_all, int bmax, double lnN) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    const int wpl = words_per_lane(bmax);
+// hist word += 1, result unused (ordering from the barriers' clobbers)
+__device__ __forceinline__ void red_add1_nc(uint32_t saddr) { asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr)); }
+
+struct Hist32Args {
+    SysDesc one;  // single-system launch (tile_sys == nullptr)
+    const SysDesc *many;
+    const PairTile *tiles;
+    const int *tile_sys;
+    int64_t n_tiles;
+    const unsigned long long *nfix;
+    double fix;
+    int *err;
+    uint32_t *ovf_all;  // per CTA: [2 * words_per_lane][32] overflow counts (units of 32,768)
+    int fc, nst, bmax;
+};
+
+// W32: 32-bit counters, word idx * 32 + lane, reduction value 1, no folding.
+// Otherwise 16-bit halves as described above.
+template <bool W32>
+__global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_constant__ Hist32Args a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int fc = a.fc, nst = a.nst;
+    const int wpl = words_per_lane(a.bmax);
     const int nwords = wpl * 32;
     uint32_t *hist = (uint32_t *)smem;
-    unsigned char *stage = smem + hist32_bytes(bmax);
-    uint64_t *full = (uint64_t *)(stage + (kStageBytes > kRedBytes ? kStageBytes : kRedBytes));
-    uint64_t *empty = full + kStages;
-    uint32_t *acc = acc_all + (size_t)blockIdx.x * 2 * nwords;  // this CTA's 32-bit counters [bin][lane]
-    __shared__ int s_abort;
+    const int fcs = fc + kPad;
+    unsigned char *stage = smem + hist32_bytes(a.bmax);
+    uint64_t *full = (uint64_t *)(stage + (size_t)nst * kNRow * fcs);
+    uint64_t *empty = full + kMaxStages;
+    __shared__ unsigned long long s_snl[32];
+    __shared__ unsigned int s_occ[32];
+    __shared__ int s_heavy[32];
+    __shared__ volatile int s_abort;   // consumers only
+    __shared__ volatile int s_pabort;  // producer
+    __shared__ long long s_issued;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int F = geo.F;
-    const int nchunks = (F + kFC - 1) / kFC;
-    const uint32_t hbase = smem_u32(hist) + lane * 4;
-
-    for (int ti = blockIdx.x; ti < n_tiles; ti += gridDim.x) {
-        const PairTile tile = tiles[ti];
-        auto row_dof = [&](int k) -> int {
-            if (k < kRows) return k < tile.nrow ? tile.row0 + k : -1;
-            return (k - kRows) < tile.ncol ? tile.col0 + (k - kRows) : -1;
-        };
-        for (int i = tid * 4; i < nwords; i += kThreads * 4) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
-        if (tid == 0) {
-            s_abort = 0;
-            for (int k = 0; k < kStages; k++) {
-                mbar_init(smem_u32(&full[k]), 1);
-                mbar_init(smem_u32(&empty[k]), kConsumers);
-            }
-            mbar_init_fence();
+    for (int i = tid * 4; i < nwords; i += kThreads * 4) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < 32) {
+        s_snl[tid] = 0ull;
+        s_occ[tid] = 0u;
+        s_heavy[tid] = 0;
+    }
+    if (tid == 0) {
+        s_abort = 0;
+        s_pabort = 0;
+        s_issued = 0;
+        for (int k = 0; k < nst; k++) {
+            mbar_init(smem_u32(&full[k]), 1);
+            mbar_init(smem_u32(&empty[k]), kConsumers);
         }
-        __syncthreads();
+        mbar_init_fence();
+    }
+    __syncthreads();
 
-        bool flushed = false;  // uniform over the consumer warps
-        if (warp == kConsumers) {
-            if (lane == 0) {
-                for (int chunk = 0; chunk < nchunks; chunk++) {
-                    const int st = chunk % kStages;
-                    if (chunk >= kStages &&
-                        !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((chunk / kStages) - 1) & 1))) {
-                        s_abort = 1;
-                        break;
+    auto sys_of = [&](int64_t t) -> const SysDesc & { return a.tile_sys ? a.many[a.tile_sys[t]] : a.one; };
+
+    if (warp == kConsumers) {
+        // ---------------------------------------------------------- producer
+        // lane 0 waits for a free stage and arms its full barrier; lanes
+        // 0..kNRow-1 then issue one row copy each, in parallel
+        long long seq = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < a.n_tiles && ok; t += gridDim.x) {
+            const SysDesc &d = sys_of(t);
+            const PairTile tile = a.tiles[t];
+            const int nchunks = (d.geo.F + fc - 1) / fc;
+            const uint8_t *src = nullptr;
+            if (lane < kNRow) {
+                const int k = lane;
+                const int g = k < kRows ? (k < tile.nrow ? tile.row0 + k : -1)
+                                    : ((k - kRows) < tile.ncol ? tile.col0 + (k - kRows) : -1);
+                src = g >= 0 ? d.bins + (int64_t)g * d.geo.ldb : nullptr;
+            }
+            const uint32_t bytes = (uint32_t)__popc(__ballot_sync(0xffffffffu, src != nullptr)) * (uint32_t)fc;
+            for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
+                const int st = (int)(seq % nst);
+                int go = 1;
+                if (lane == 0) {
+                    if (seq >= nst &&
+                        !mbar_wait_bounded(smem_u32(&empty[st]), (uint32_t)(((seq / nst) - 1) & 1))) {
+                        s_pabort = 1;
+                        go = 0;
+                    } else if (s_abort) {  // the consumers gave up: stop issuing
+                        go = 0;
                     }
+                    if (go) mbar_expect_tx(smem_u32(&full[st]), bytes);
+                }
+                if (!__shfl_sync(0xffffffffu, go, 0)) {
+                    ok = false;
+                    break;
+                }
+                if (src) {
+                    // generic-proxy reads of this stage (released by the empty
+                    // barrier) before the async-proxy writes refilling it
                     fence_proxy_async();
-                    uint32_t bytes = 0;
-                    for (int k = 0; k < kNRow; k++) bytes += row_dof(k) >= 0 ? (uint32_t)kFC : 0u;
-                    const uint32_t bar = smem_u32(&full[st]);
-                    mbar_expect_tx(bar, bytes);
-                    for (int k = 0; k < kNRow; k++) {
-                        const int g = row_dof(k);
-                        if (g < 0) continue;
-                        bulk_g2s(smem_u32(stage + (size_t)(st * kNRow + k) * kFCS),
-                                 bins + (int64_t)g * geo.ldb + (int64_t)chunk * kFC, (uint32_t)kFC, bar);
-                    }
+                    bulk_g2s(smem_u32(stage + (size_t)(st * kNRow + lane) * fcs), src + (int64_t)chunk * fc,
+                             (uint32_t)fc, smem_u32(&full[st]));
                 }
             }
-        } else {
-            const int pr = lane / kCols, pc = lane % kCols;
+        }
+        if (lane == 0) s_issued = seq;
+    } else {
+        // --------------------------------------------------------- consumers
+        const int pr = lane / kCols, pc = lane % kCols;
+        const uint32_t hbase = smem_u32(hist) + lane * 4;
+        uint32_t *ovf = a.ovf_all + (size_t)blockIdx.x * 2 * nwords;  // [bin][lane]
+        const int gstep = (fc / 16) % kConsumers;
+        const int fold_every = kFoldFrames / fc;  // chunks between folds
+        const int ctid = tid;
+        const int ew = ctid >> 5;  // epilogue / fold: words j = ew + 31 k of slot `lane`
+        long long seq = 0;
+        for (int64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+            const SysDesc &d = sys_of(t);
+            const PairTile tile = a.tiles[t];
+            const int F = d.geo.F;
+            const int nchunks = (F + fc - 1) / fc;
             const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
             const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
             const bool valid = gr >= 0 && gc >= 0 && gr < gc;
-            const uint32_t Bc = valid ? (uint32_t)dof.b2[gc] : 0u;
-            // 16-frame groups round-robin over the consumer warps, rotating the
-            // leftover groups from chunk to chunk
-            const int gstep = (kFC / 16) % kConsumers;
+            const uint32_t Bc = valid ? (uint32_t)d.dof.b2[gc] : 0u;
+            // every warp holds all 32 slots, so this vote is the same in all
+            // consumer warps (it decides who takes the fold barriers)
+            const bool risky = valid && min(d.dof.m2[gr], d.dof.m2[gc]) > 65535;
+            const bool folding = !W32 && __any_sync(0xffffffffu, risky) && nchunks > fold_every;
             int g0 = warp;
-            // A warp whose wait timed out stops waiting and counting but keeps
-            // going through the chunks, so that it still reaches every
-            // window barrier of the other consumer warps.
-            bool dead = false;
-            for (int chunk = 0; chunk < nchunks; chunk++) {
-                const int st = chunk % kStages;
-                if (!dead && !mbar_wait_bounded(smem_u32(&full[st]), (uint32_t)((chunk / kStages) & 1))) {
-                    dead = true;
+            bool dead = false;  // a timed-out warp keeps taking the fold barriers
+            for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
+                const int st = (int)(seq % nst);
+                if (!dead && !mbar_wait_bounded(smem_u32(&full[st]), (uint32_t)((seq / nst) & 1))) {
                     s_abort = 1;
+                    dead = true;
                 }
-                const int fvalid = min(kFC, F - chunk * kFC);
-                const unsigned char *rrow = stage + (size_t)(st * kNRow + pr) * kFCS;
-                const unsigned char *crow = stage + (size_t)(st * kNRow + kRows + pc) * kFCS;
-                if (valid && !dead) {
-                    for (int off = g0 * 16; off < fvalid; off += kConsumers * 16) {
-                        const uint4 rv = *(const uint4 *)(rrow + off);
-                        const uint4 cv = *(const uint4 *)(crow + off);
-                        const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
-                        const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
-                        const int n = fvalid - off;  // frames of this group that exist
-                        if (n >= 16) {
+                if (!dead) {
+                    const int fvalid = min(fc, F - chunk * fc);
+                    const unsigned char *rrow = stage + (size_t)(st * kNRow + pr) * fcs;
+                    const unsigned char *crow = stage + (size_t)(st * kNRow + kRows + pc) * fcs;
+                    if (valid) {
+                        for (int off = g0 * 16; off < fvalid; off += kConsumers * 16) {
+                            const uint4 rv = *(const uint4 *)(rrow + off);
+                            const uint4 cv = *(const uint4 *)(crow + off);
+                            const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                            const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                            if (off + 16 <= fvalid) {
+                                // two frames per IMAD (idx < 2500 never carries into
+                                // the upper half); word idx >> 1 of this lane, half idx & 1
+                                uint32_t ix[8];
 #pragma unroll
-                            for (int q = 0; q < 4; q++) {
-                                // two frames per IMAD (idx < 2500 never carries into the upper half);
-                                // word (idx >> 1) of this lane, half idx & 1
-                                const uint32_t i01 = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
-                                const uint32_t i23 = __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
-                                red_add_nc(hbase + ((i01 & 0xfffeu) << 6), (i01 & 1u) * 0xffffu + 1u);
-                                red_add_nc(hbase + ((i01 >> 17) << 7), ((i01 >> 16) & 1u) * 0xffffu + 1u);
-                                red_add_nc(hbase + ((i23 & 0xfffeu) << 6), (i23 & 1u) * 0xffffu + 1u);
-                                red_add_nc(hbase + ((i23 >> 17) << 7), ((i23 >> 16) & 1u) * 0xffffu + 1u);
-                            }
-                        } else {  // ragged end of the trajectory
+                                for (int q = 0; q < 4; q++) {
+                                    ix[2 * q] = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
+                                    ix[2 * q + 1] =
+                                        __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
+                                }
+                                // frames in the order 0, 4, 8, 12, 1, 5, ...: consecutive
+                                // reductions of a lane are four frames apart, so runs of
+                                // one bin in correlated trajectories do not queue
+                                // read-modify-writes on one word back to back
 #pragma unroll
-                            for (int k = 0; k < 16; k++) {
-                                if (k < n) {
-                                    const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                                    const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                                    const uint32_t idx = br * Bc + bc;
-                                    red_add_nc(hbase + ((idx >> 1) << 7), (idx & 1u) * 0xffffu + 1u);
+                                for (int k = 0; k < 4; k++) {
+#pragma unroll
+                                    for (int q = 0; q < 4; q++) {
+                                        const uint32_t v = ix[2 * q + (k >> 1)];
+                                        if (W32)
+                                            red_add1_nc(hbase + (((k & 1) ? (v >> 16) : (v & 0xffffu)) << 7));
+                                        else if (k & 1)
+                                            red_add_nc(hbase + ((v >> 17) << 7), ((v >> 16) & 1u) * 0xffffu + 1u);
+                                        else
+                                            red_add_nc(hbase + ((v & 0xfffeu) << 6), (v & 1u) * 0xffffu + 1u);
+                                    }
+                                }
+                            } else {  // ragged end of the trajectory
+                                const int n = fvalid - off;
+#pragma unroll
+                                for (int k = 0; k < 16; k++) {
+                                    if (k < n) {
+                                        const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                        const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                                        const uint32_t idx = br * Bc + bc;
+                                        if (W32) red_add1_nc(hbase + (idx << 7));
+                                        else red_add_nc(hbase + ((idx >> 1) << 7), (idx & 1u) * 0xffffu + 1u);
+                                    }
                                 }
                             }
                         }
                     }
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive_relaxed(smem_u32(&empty[st]));
                 }
-                __syncwarp();
-                if (lane == 0) mbar_arrive_relaxed(smem_u32(&empty[st]));
                 g0 -= gstep;
                 if (g0 < 0) g0 += kConsumers;
-                if ((chunk + 1) % kWindowChunks == 0 && chunk + 1 < nchunks) {
-                    // fold the 16-bit halves into the 32-bit accumulator before
-                    // any can reach 65,536; the barrier also drains the
-                    // consumers' outstanding reductions
-                    named_barrier(kConsumers * 32);
-                    for (int w = tid; w < nwords; w += kConsumers * 32) {
+                if (folding && (chunk + 1) % fold_every == 0 && chunk + 1 < nchunks) {
+                    // every consumer's reductions so far are done; move
+                    // 32,768 out of each counter that reached it
+                    named_barrier(kConsumerThreads);
+                    for (int w = ctid; w < nwords; w += kConsumerThreads) {
                         const uint32_t v = hist[w];
-                        hist[w] = 0u;
-                        const int b2 = (w >> 5) * 2, l = w & 31;
-                        uint32_t *a = acc + (size_t)b2 * 32 + l;
-                        if (flushed) {
-                            a[0] += v & 0xffffu;
-                            a[32] += v >> 16;
-                        } else {
-                            a[0] = v & 0xffffu;
-                            a[32] = v >> 16;
+                        if (v & 0x80008000u) {
+                            const uint32_t lo = (v >> 15) & 1u, hi = v >> 31;
+                            hist[w] = v - (lo << 15) - (hi << 31);
+                            const int b = (w >> 5) * 2;
+                            if (lo) ovf[b * 32 + lane] += 1u;
+                            if (hi) ovf[(b + 1) * 32 + lane] += 1u;
+                            s_heavy[lane] = 1;
                         }
                     }
-                    flushed = true;
-                    named_barrier(kConsumers * 32);
+                    named_barrier(kConsumerThreads);
                 }
             }
-        }
-        // consumers tell everyone whether the accumulator holds earlier windows
-        const int any_flush = __syncthreads_or(flushed ? 1 : 0);
-        if (s_abort) {
-            if (tid == 0) {
-                atomicAdd(&err[ERR_TIMEOUT], 1);
-                for (int c = 0; c < kStages; c++) (void)mbar_wait_bounded(smem_u32(&full[c]), 0u);
-            }
-            __syncthreads();
-            return;
-        }
+            named_barrier(kConsumerThreads);
+            if (s_abort) break;  // the same value for every consumer
 
-        // ---- epilogue: thread t handles pair slot t % 32 and bins t/32, +32, ...
-        const int el = tid & 31, ew = tid >> 5;
-        const int er = el / kCols, ec = el % kCols;
-        const int egr = er < tile.nrow ? tile.row0 + er : -1;
-        const int egc = ec < tile.ncol ? tile.col0 + ec : -1;
-        const bool evalid = egr >= 0 && egc >= 0 && egr < egc;
-        double snl = 0.0;
-        int occ = 0;
-        if (evalid) {
-            const int nbin = dof.b2[egr] * dof.b2[egc];
-            int64_t *dump = out.counts ? out.counts + ((int64_t)ti * 32 + el) * out.counts_bmax * out.counts_bmax : nullptr;
-            for (int b = ew; b < nbin; b += kWarps) {
-                uint32_t n = (hist[(b >> 1) * 32 + el] >> ((b & 1) * 16)) & 0xffffu;
-                if (any_flush) n += acc[(size_t)b * 32 + el];
-                if (n) {
-                    snl += __ldg(nlogn + n);
-                    occ++;
+            // ---- epilogue: this thread reads words j = ew, ew + 31, ... of
+            // slot `lane` (the words its folds handled), zeroing them
+            const int egr = gr, egc = gc;
+            unsigned long long snl = 0ull;
+            int occ = 0;
+            if (valid && W32) {
+                const int nbin = d.dof.b2[egr] * d.dof.b2[egc];
+                int64_t *dump = d.out.counts ? d.out.counts + (t * 32 + lane) * d.out.counts_bmax * d.out.counts_bmax
+                                             : nullptr;
+                for (int j = ew; j < nbin; j += kConsumers) {
+                    const int w = j * 32 + lane;
+                    const uint32_t n = hist[w];
+                    hist[w] = 0u;
+                    snl += __ldg(a.nfix + n);
+                    occ += n != 0u;
+                    if (dump) dump[j] = n;
                 }
-                if (dump) dump[b] = n;
+                atomicAdd(&s_snl[lane], snl);
+                atomicAdd(&s_occ[lane], (unsigned int)occ);
+            } else if (valid) {
+                const int nbin = d.dof.b2[egr] * d.dof.b2[egc];
+                const int nw = (nbin + 1) / 2;
+                const bool heavy = s_heavy[lane] != 0;
+                int64_t *dump = d.out.counts ? d.out.counts + (t * 32 + lane) * d.out.counts_bmax * d.out.counts_bmax
+                                             : nullptr;
+                for (int j = ew; j < nw; j += kConsumers) {
+                    const int w = j * 32 + lane;
+                    const uint32_t v = hist[w];
+                    hist[w] = 0u;
+                    uint32_t n0 = v & 0xffffu, n1 = v >> 16;
+                    if (heavy) {
+                        uint32_t *o = ovf + (size_t)(2 * j) * 32 + lane;
+                        const uint32_t o0 = o[0], o1 = o[32];
+                        if (o0 | o1) {
+                            n0 += o0 << 15;
+                            n1 += o1 << 15;
+                            o[0] = 0u;
+                            o[32] = 0u;
+                        }
+                    }
+                    snl += __ldg(a.nfix + n0) + __ldg(a.nfix + n1);
+                    occ += (n0 != 0u) + (n1 != 0u);
+                    if (dump) {
+                        dump[2 * j] = n0;
+                        if (2 * j + 1 < nbin) dump[2 * j + 1] = n1;
+                    }
+                }
+                atomicAdd(&s_snl[lane], snl);
+                atomicAdd(&s_occ[lane], (unsigned int)occ);
+            }
+            named_barrier(kConsumerThreads);
+            if (ctid < 32) {
+                if (valid) {
+                    const double N = (double)F;
+                    const double sn = (double)s_snl[ctid] / a.fix;
+                    const int o = (int)s_occ[ctid];
+                    const double S2 = d.lnN + d.dof.acon[egr] + d.dof.acon[egc] - sn / N + (o - 1.0) / (2.0 * N);
+                    if (d.out.par) d.out.par[par_pair_index(d.out.L, d.geo.nb, d.geo.na, d.geo.nd, egr, egc)] = S2;
+                    if (d.out.mi) {
+                        const double mi = d.dof.s1[egr] + d.dof.s1[egc] - S2;
+                        d.out.mi[(int64_t)egr * d.geo.D + egc] = mi;
+                        d.out.mi[(int64_t)egc * d.geo.D + egr] = mi;
+                    }
+                }
+                s_snl[ctid] = 0ull;
+                s_occ[ctid] = 0u;
+                s_heavy[ctid] = 0;
             }
         }
-        double *red_snl = (double *)stage;                // [kWarps][32]
-        int *red_occ = (int *)(red_snl + kWarps * 32);    // [kWarps][32]
-        red_snl[ew * 32 + el] = snl;
-        red_occ[ew * 32 + el] = occ;
+    }
+    __syncthreads();
+
+    if (s_abort || s_pabort) {
+        if (tid == 0) {
+            atomicAdd(&a.err[ERR_TIMEOUT], 1);
+            const long long n = s_issued;
+            for (long long k = n > nst ? n - nst : 0; k < n; k++)
+                (void)mbar_wait_bounded(smem_u32(&full[k % nst]), (uint32_t)((k / nst) & 1));
+        }
         __syncthreads();
-        if (tid < 32) {
-            const int pr2 = tid / kCols, pc2 = tid % kCols;
-            const int g1 = pr2 < tile.nrow ? tile.row0 + pr2 : -1;
-            const int g2 = pc2 < tile.ncol ? tile.col0 + pc2 : -1;
-            if (g1 >= 0 && g2 >= 0 && g1 < g2) {
-                double s = 0.0;
-                int o = 0;
-                for (int w = 0; w < kWarps; w++) {
-                    s += red_snl[w * 32 + tid];
-                    o += red_occ[w * 32 + tid];
-                }
-                const double N = (double)F;
-                const double S2 = lnN + dof.acon[g1] + dof.acon[g2] - s / N + (o - 1.0) / (2.0 * N);
-                if (out.par) out.par[par_pair_index(out.L, geo.nb, geo.na, geo.nd, g1, g2)] = S2;
-                if (out.mi) {
-                    const double mi = dof.s1[g1] + dof.s1[g2] - S2;
-                    out.mi[(int64_t)g1 * geo.D + g2] = mi;
-                    out.mi[(int64_t)g2 * geo.D + g1] = mi;
-                }
-            }
-        }
-        __syncthreads();  // smem (counters, stages, barriers) is reused by the next tile
     }
 }
 
-size_t smem_bytes(int bmax) {
-    return hist32_bytes(bmax) + (kStageBytes > kRedBytes ? kStageBytes : kRedBytes) + 8 * 2 * kStages;
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    }
+    return n;
+}
+
+// Staging geometry for a bin count: frames per chunk x stages, the largest
+// chunks that fit (measured at 30 bins: 11.2, 13.3 and 14.2 updates/clock/SM
+// for 1,024-, 2,048- and 4,096-frame chunks), at most 4096 frames (the
+// padding of every bin row). PG_HIST32_FC / PG_HIST32_STAGES override it for
+// sweeps when they fit.
+bool config(int bmax, int *fc, int *nst) {
+    static const int cand[][2] = {{4096, 2}, {2048, 4}, {2048, 3}, {2048, 2}, {1024, 4}, {1024, 2}};
+    int ofc = 0, onst = 0;
+    if (const char *e = getenv("PG_HIST32_FC")) ofc = atoi(e);
+    if (const char *e = getenv("PG_HIST32_STAGES")) onst = atoi(e);
+    if (ofc >= 256 && ofc <= 4096 && ofc % 16 == 0 && onst >= 2 && onst <= kMaxStages &&
+        smem_bytes(bmax, ofc, onst) + 1024 <= (size_t)kSmemMax) {
+        *fc = ofc;
+        *nst = onst;
+        return true;
+    }
+    for (const auto &c : cand)
+        if (smem_bytes(bmax, c[0], c[1]) + 1024 <= (size_t)kSmemMax) {
+            *fc = c[0];
+            *nst = c[1];
+            return true;
+        }
+    return false;
+}
+
+cudaError_t launch(Hist32Args &a, void *scratch, size_t scratch_bytes, cudaStream_t st) {
+    if (!config(a.bmax, &a.fc, &a.nst)) return cudaErrorInvalidValue;
+    if (a.n_tiles <= 0) return cudaSuccess;
+    const int grid = (int)std::min<int64_t>(a.n_tiles, sm_count());
+    const size_t need = pairs_hist32_scratch_bytes(a.bmax, grid);
+    if (!scratch || scratch_bytes < need) return cudaErrorInvalidValue;
+    cudaError_t e = wide_counters(a.bmax) ? cudaSuccess : cudaMemsetAsync(scratch, 0, need, st);
+    if (e != cudaSuccess) return e;
+    a.ovf_all = (uint32_t *)scratch;
+    const size_t smem = smem_bytes(a.bmax, a.fc, a.nst);
+    if (wide_counters(a.bmax)) {
+        e = cudaFuncSetAttribute(pairs_hist32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pairs_hist32_kernel<true><<<grid, kThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(pairs_hist32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        pairs_hist32_kernel<false><<<grid, kThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
 }
 
 }  // namespace
 
-bool pairs_hist32_supported(int bmax) { return bmax <= kBmax && smem_bytes(bmax) + 1024 <= (size_t)kSmemMax; }
+bool pairs_hist32_supported(int bmax) {
+    int fc = 0, nst = 0;
+    return bmax >= 1 && bmax <= kBmax16 && config(bmax, &fc, &nst);
+}
 
-// accumulator bytes for `grid` CTAs
+bool pairs_hist32_wide(int bmax) { return pairs_hist32_supported(bmax) && wide_counters(bmax); }
+
+int pairs_hist32_grid(int64_t n_tiles) { return (int)std::max<int64_t>(1, std::min<int64_t>(n_tiles, sm_count())); }
+
+// overflow-count bytes for `grid` CTAs
 size_t pairs_hist32_scratch_bytes(int bmax, int grid) {
+    if (wide_counters(bmax)) return 256;  // 32-bit counters never move counts out
     return (size_t)grid * 2 * words_per_lane(bmax) * 32 * sizeof(uint32_t);
 }
 
@@ -282,21 +455,42 @@ std::vector<PairTile> build_tiles32(int D) {
     return t;
 }
 
-cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, const double *nlogn,
-                                const PairTile *tiles, int64_t n_tiles, int grid, PairOut out, int *err,
-                                void *scratch, size_t scratch_bytes, cudaStream_t st) {
+cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                                const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
+                                PairOut out, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st) {
     int bmax = 1;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (!pairs_hist32_supported(bmax) || n_tiles > INT32_MAX || grid < 1) return cudaErrorInvalidValue;
-    if (scratch_bytes < pairs_hist32_scratch_bytes(bmax, grid)) return cudaErrorInvalidValue;
-    if ((int64_t)g.ldb < (int64_t)((g.F + kFC - 1) / kFC) * kFC) return cudaErrorInvalidValue;
-    if (n_tiles <= 0) return cudaSuccess;
-    const size_t smem = smem_bytes(bmax);
-    cudaError_t e = cudaFuncSetAttribute(pairs_hist32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    pairs_hist32_kernel<<<grid, kThreads, smem, st>>>(g, bins, dof, nlogn, tiles, (int)n_tiles, out, err,
-                                                      (uint32_t *)scratch, bmax, log((double)g.F));
-    return cudaGetLastError();
+    if (!pairs_hist32_supported(bmax)) return cudaErrorInvalidValue;
+    if (g.ldb < bins_ld(g.F)) return cudaErrorInvalidValue;
+    Hist32Args a{};
+    a.one.geo = g;
+    a.one.bins = bins;
+    a.one.dof = dof;
+    a.one.out = out;
+    a.one.lnN = log((double)g.F);
+    a.tiles = tiles;
+    a.n_tiles = n_tiles;
+    a.nfix = nfix;
+    a.fix = fix;
+    a.err = err;
+    a.bmax = bmax;
+    return launch(a, scratch, scratch_bytes, st);
+}
+
+cudaError_t launch_pairs_hist32_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
+                                      int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
+                                      void *scratch, size_t scratch_bytes, cudaStream_t st) {
+    if (!pairs_hist32_supported(bmax)) return cudaErrorInvalidValue;
+    Hist32Args a{};
+    a.many = sys;
+    a.tiles = tiles;
+    a.tile_sys = tile_sys;
+    a.n_tiles = n_tiles;
+    a.nfix = nfix;
+    a.fix = fix;
+    a.err = err;
+    a.bmax = bmax;
+    return launch(a, scratch, scratch_bytes, st);
 }
 
 }  // namespace pg

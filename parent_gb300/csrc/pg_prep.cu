@@ -397,7 +397,7 @@ __global__ void nlogn_kernel(double *t, int nmax) {
 
 __global__ void nlogn_fix_kernel(unsigned long long *t, int nmax, double fix) {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
-        t[n] = n > 1 ? (unsigned long long)llrint((double)n * log((double)n) * fix) : 0ull;
+        t[n] = n > 1 ? __double2ull_rn((double)n * log((double)n) * fix) : 0ull;  // unsigned: entries reach 1.6e19
 }
 
 }  // namespace

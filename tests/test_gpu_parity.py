@@ -329,10 +329,11 @@ def test_large_properties(eng):
     assert len(seen) == D
 
 
-@pytest.mark.parametrize("n_atoms,F,bins", [(40, 70000, (50,) * 6), (20, 3000, (10, 20, 30, 50, 20, 8))])
+@pytest.mark.parametrize("n_atoms,F,bins", [(40, 70000, (50,) * 6), (20, 3000, (10, 20, 30, 50, 20, 8)),
+                                            (30, 20000, (30,) * 6), (25, 5000, (20, 30, 35, 35, 20, 8))])
 def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
-    """The 32-slot histogram layout (16-bit counters folded into 32-bit every
-    63,488 frames; F = 70,000 crosses one fold) gives the same counts and values."""
+    """The 32-slot histogram layout (32-bit counters up to 35 bins, 16-bit
+    halves above) gives the same counts and values."""
     monkeypatch.setenv("PG_HIST_SLOTS", "32")
     t = _synth_case(n_atoms, F, 0, seed=n_atoms + F, frac_bimodal_dih=0.2)
     body = eng.entropy(t, bins, "hist")
@@ -425,4 +426,49 @@ def test_fp32_bin_edges_bit_exact(eng):
     assert np.array_equal(sh.view(np.uint64), osh.view(np.uint64))
     body = eng.entropy(traj, bins, "hist")
     ref = oracle.parent(bonds, angles, dih, bins)
+    compare_bodies(n_dih, body, ref)
+
+
+def test_hist16_layout_matches_oracle(eng, monkeypatch):
+    """The 16-slot histogram layout (32-bit counters, two lanes per pair),
+    forced at 50 bins where the 32-slot layout is the default."""
+    monkeypatch.setenv("PG_HIST_SLOTS", "16")
+    t = _synth_case(40, 30000, 0, seed=99, frac_bimodal_dih=0.2)
+    body = eng.entropy(t, (50,) * 6, "hist")
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6)
+    compare_bodies(37, body, ref)
+    D = 3 * 40 - 6
+    pairs = [(0, 1), (0, D - 1), (5, 17), (D - 2, D - 1)]
+    got = eng.pair_counts(t, (50,) * 6, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, (50,) * 6, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
+
+
+@pytest.mark.parametrize("slots", ["32", "16"])
+def test_peaked_counts_above_16_bits(eng, monkeypatch, slots):
+    """Pairs of DOFs that sit on one value in the same 70% of 150,000 frames:
+    one 2D bin holds 105,000 counts, above a 16-bit counter, so the 32-slot
+    layout has to move counts out during the run. Counts stay bit-exact."""
+    monkeypatch.setenv("PG_HIST_SLOTS", slots)
+    rng = np.random.default_rng(5)
+    n_dih, F = 5, 150000
+    t = pg.synth_host(n_dih + 3, F, double_prec=0, seed=77)
+    peak = rng.random(F) < 0.7
+    t.bonds[0, peak] = np.float32(0.15)
+    t.bonds[3, peak] = np.float32(0.16)
+    t.angles[2, peak] = np.float32(1.9)
+    t.dihedrals[1, peak] = np.float32(2.5)
+    t.dihedrals[4, peak[::-1]] = np.float32(1.0)   # a different 70%
+    nb, na = n_dih + 2, n_dih + 1
+    D = nb + na + n_dih
+    peaked = [0, 3, nb + 2, nb + na + 1, nb + na + 4]
+    pairs = sorted({tuple(sorted((a, b))) for a in peaked for b in range(D) if a != b})
+    got = eng.pair_counts(t, (50,) * 6, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, (50,) * 6, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
+    assert max(int(x.max()) for x in want) > 65535
+    body = eng.entropy(t, (50,) * 6, "hist")
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6)
     compare_bodies(n_dih, body, ref)
