@@ -117,6 +117,9 @@ struct pg_ctx {
     DevBuf batch, batchmeta;
     cudaGraphExec_t graph = nullptr;
     std::vector<int64_t> graph_key;
+    // host trajectories: uploads run on their own stream, one event per DOF group
+    cudaStream_t copy = nullptr;
+    cudaEvent_t gev[16] = {};
 };
 
 static int fail(pg_ctx *c, int code, const char *fmt, ...) {
@@ -152,9 +155,8 @@ static DofArrays dof_arrays(pg_ctx *ctx, int D) {
 
 static size_t elem_size(int prec) { return prec ? 8 : 4; }
 
-// Shared front half of pg_entropy / pg_pair_counts: validation, upload,
-// preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
-static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
+// Validation and the geometry of a trajectory (ctx->geo).
+static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     if (!tv || !bins) return fail(ctx, PG_ERR_ARG, "null trajectory or bins");
     if (tv->n_dihedrals < 0 || tv->n_frames < 1)
         return fail(ctx, PG_ERR_ARG, "n_dihedrals (%d) < 0 or n_frames (%d) < 1", tv->n_dihedrals, tv->n_frames);
@@ -180,6 +182,15 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     g.ldb = bins_ld(g.F);
     for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
     ctx->resident = false;
+    return PG_OK;
+}
+
+// Shared front half of pg_entropy / pg_pair_counts: validation, upload,
+// preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
+static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
+    int rc0 = setup_geometry(ctx, tv, bins);
+    if (rc0) return rc0;
+    const SysGeom &g = ctx->geo;
     const int D = g.D;
     cudaStream_t st = ctx->stream;
 
@@ -317,6 +328,136 @@ static int run_hist32(pg_ctx *ctx, const SysGeom &g, const DofArrays &dof, const
 static int mist_edges_to_user(pg_ctx *ctx, int n_dihedrals, const double *hmi, const int *hf, const int *ht,
                               const double *s1, pg_mist_edge *edges, double totals[10]);
 
+// Entropies of a HOST trajectory with the upload overlapped: the DOFs are
+// split into up to 16 groups on column super-block boundaries of the tile
+// list; a second stream uploads group after group, and on the context's
+// stream group k's preprocessing and the pair tiles whose column block lies
+// in group k (their row DOFs are in groups <= k) start as soon as group k has
+// arrived. Same kernels and results as the device-resident path; histogram
+// form (geometry already set by setup_geometry).
+static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
+    const SysGeom &g = ctx->geo;
+    const int D = g.D;
+    cudaStream_t st = ctx->stream, cs = ctx->copy;
+    const size_t es = elem_size(tv->double_prec);
+    const int64_t F = g.F;
+    const bool h32 = use_hist32(g);
+    int T = 0, fc = 0, nst = 0;
+    if (!h32 && !pairs_hist_config(bmax_of(g), &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+    if (prep_smem_bytes(g) > 200 * 1024) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin counts too large");
+    const ParLayout L = par_layout(g.n_dih);
+    CK(ctx->cols.ensure((size_t)D * F * es + 256));
+    CK(ctx->bins.ensure((size_t)D * g.ldb));
+    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
+    CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
+    CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
+    CK(ctx->mi.ensure((size_t)D * D * sizeof(double)));
+    const int layout = h32 ? 32 : T;
+    if (ctx->tiles_D != D || ctx->tiles_T != layout) {
+        ctx->tiles_host = h32 ? build_tiles32(D) : build_tiles(D, T);
+        CK(ctx->tiles.ensure(ctx->tiles_host.size() * sizeof(PairTile)));
+        CK(cudaMemcpyAsync(ctx->tiles.p, ctx->tiles_host.data(), ctx->tiles_host.size() * sizeof(PairTile),
+                           cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        ctx->tiles_D = D;
+        ctx->tiles_T = layout;
+    }
+    // groups of whole column super-blocks (16 tiles wide); both tile lists
+    // run over column super-blocks in order, so a group's tiles are one range
+    const int sbw = 16 * (h32 ? 8 : T);
+    const int nsb = (D + sbw - 1) / sbw;
+    const int K = std::min(16, nsb);
+    std::vector<int> G((size_t)K + 1);
+    std::vector<int64_t> cut((size_t)K + 1);
+    for (int k = 0; k <= K; k++) G[k] = std::min(D, (int)((int64_t)k * nsb / K) * sbw);
+    {
+        const std::vector<PairTile> &tl = ctx->tiles_host;
+        int64_t i = 0;
+        for (int k = 0; k <= K; k++) {
+            while (i < (int64_t)tl.size() && tl[i].col0 < G[k]) i++;
+            cut[k] = k == K ? (int64_t)tl.size() : i;
+        }
+    }
+    const size_t sb32 = h32 ? pairs_hist32_scratch_bytes(bmax_of(g), pairs_hist32_grid((int64_t)ctx->tiles_host.size()))
+                            : 0;
+    if (h32) CK(ctx->scratch.ensure(sb32));
+
+    CK(cudaEventRecord(ctx->ev[0], st));
+    CK(cudaStreamWaitEvent(cs, ctx->ev[0], 0));  // earlier kernels reading the columns are done
+    char *cols = (char *)ctx->cols.p;
+    const int lo[3] = {0, g.nb, g.nb + g.na}, cnt[3] = {g.nb, g.na, g.nd};
+    const void *src[3] = {tv->bonds, tv->angles, tv->dihedrals};
+    for (int k = 0; k < K; k++) {
+        for (int t = 0; t < 3; t++) {
+            const int a = std::max(G[k], lo[t]), b = std::min(G[k + 1], lo[t] + cnt[t]);
+            if (a >= b) continue;
+            CK(cudaMemcpy2DAsync(cols + (size_t)a * F * es, (size_t)F * es,
+                                 (const char *)src[t] + (size_t)(a - lo[t]) * tv->ld * es, (size_t)tv->ld * es,
+                                 (size_t)F * es, (size_t)(b - a), cudaMemcpyHostToDevice, cs));
+        }
+        CK(cudaEventRecord(ctx->gev[k], cs));
+    }
+    CK(cudaEventRecord(ctx->ev[4], cs));
+
+    CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
+    int rc = ensure_fix_table(ctx, g.F);
+    if (rc) return rc;
+    const void *colp[3] = {cols, cols + (size_t)g.nb * F * es,
+                           g.nd ? cols + (size_t)(g.nb + g.na) * F * es : cols + (size_t)g.nb * F * es};
+    const DofArrays dof = dof_arrays(ctx, D);
+    PairOut po;
+    po.par = (double *)ctx->par.p;
+    po.mi = (double *)ctx->mi.p;
+    po.L = L;
+    po.counts = nullptr;
+    po.counts_bmax = 0;
+    const PairTile *tiles = (const PairTile *)ctx->tiles.p;
+    for (int k = 0; k < K; k++) {
+        CK(cudaStreamWaitEvent(st, ctx->gev[k], 0));
+        CK(launch_prep(g, colp, F, tv->double_prec, dof, (uint8_t *)ctx->bins.p, (int *)ctx->errw.p, st, G[k],
+                       G[k + 1] - G[k]));
+        ctx->launches++;
+        const int64_t n = cut[k + 1] - cut[k];
+        if (n <= 0) continue;
+        if (h32)
+            CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                                   ctx->nfix_scale, tiles + cut[k], n, po, (int *)ctx->errw.p, ctx->scratch.p, sb32,
+                                   st));
+        else
+            CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                                 ctx->nfix_scale, tiles + cut[k], n, T, po, (int *)ctx->errw.p, st));
+        ctx->launches++;
+    }
+    CK(cudaMemcpyAsync((double *)ctx->par.p + L.s1b, dof.s1, (size_t)D * sizeof(double), cudaMemcpyDeviceToDevice,
+                       st));
+    CK(cudaEventRecord(ctx->ev[1], st));
+    if (out) {
+        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
+        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
+        for (int k = 0; k < 9; k++) {
+            const int64_t n = off[k + 1] - off[k];
+            if (n <= 0) continue;
+            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
+            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+        }
+    }
+    CK(cudaEventRecord(ctx->ev[2], st));
+    rc = check_err_words(ctx);
+    float up = 0.f, dev = 0.f, down = 0.f;
+    cudaEventElapsedTime(&up, ctx->ev[0], ctx->ev[4]);
+    cudaEventElapsedTime(&dev, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&down, ctx->ev[1], ctx->ev[2]);
+    ctx->timings[0] = 0.0;   // preprocessing runs interleaved with the pair launches
+    ctx->timings[1] = dev;   // first upload group to the last pair launch
+    ctx->timings[3] = up + down;
+    ctx->timings[4] = dev + down;
+    if (rc) return rc;
+    ctx->last_form = PG_FORM_HIST;
+    ctx->resident = true;
+    return PG_OK;
+}
+
 extern "C" {
 
 PG_API const char *pg_last_global_error(void) { return g_global_err.c_str(); }
@@ -334,7 +475,9 @@ PG_API int pg_create(pg_ctx **out, int device) {
     pg_ctx *c = new pg_ctx;
     c->device = device;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
     for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaEventCreate(&c->ev[k]);
+    for (int k = 0; k < 16 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&c->gev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(nullptr, PG_ERR_CUDA, "stream/event creation: %s", cudaGetErrorString(e));
@@ -353,9 +496,13 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->batch.release();
     ctx->batchmeta.release();
+    if (ctx->copy) cudaStreamSynchronize(ctx->copy);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->gev)
+        if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->copy) cudaStreamDestroy(ctx->copy);
     delete ctx;
 }
 
@@ -366,6 +513,12 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
     if (form < PG_FORM_AUTO || form > PG_FORM_ONEHOT) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    if (traj && !traj->on_device && form != PG_FORM_ONEHOT) {
+        int rc0 = setup_geometry(ctx, traj, bins);
+        if (rc0) return rc0;
+        const int f = form == PG_FORM_AUTO ? autotune_form(ctx->geo) : form;
+        if (f != PG_FORM_ONEHOT || !pairs_onehot_supported(ctx->geo)) return run_streamed(ctx, traj, out);
+    }
     int rc = run_prep(ctx, traj, bins);
     if (rc) return rc;
     const SysGeom &g = ctx->geo;

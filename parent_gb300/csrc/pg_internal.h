@@ -84,10 +84,12 @@ cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st);
 // for some F >= nmax (fixed point, so sums are exact integer additions).
 cudaError_t launch_nlogn_fix_table(unsigned long long *nfix, int nmax, double fix, cudaStream_t st);
 
-// Extrema + modfit + binning + 1D entropies + 2D decomposition constants.
+// Extrema + modfit + binning + 1D entropies + 2D decomposition constants for
+// DOFs [g_first, g_first + g_count) (g_count < 0: through the last DOF).
 // cols[t] = device base of the type-t block (columns ld elements apart).
 cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
-                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st);
+                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st, int g_first = 0,
+                        int g_count = -1);
 
 // Shared-memory histogram pair kernel with fused entropy/MI epilogue.
 // If counts != nullptr the raw 2D histograms of each tile's first pair slots

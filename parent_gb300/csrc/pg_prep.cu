@@ -79,9 +79,9 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
                                                         const void *ca, const void *cd,
                                                         int64_t ld, int prec, DofArrays dof,
                                                         uint8_t *bins, int *err,
-                                                        double modfit_bs, double pi) {
+                                                        double modfit_bs, double pi, int g_first) {
     extern __shared__ unsigned int sh[];
-    const int g = blockIdx.x;
+    const int g = g_first + blockIdx.x;
     const int type = dof_type(g, geo.nb, geo.na);
     const int local = g - (type == TB ? 0 : (type == TA ? geo.nb : geo.nb + geo.na));
     const void *col = type == TB ? cb : (type == TA ? ca : cd);
@@ -426,14 +426,18 @@ size_t prep_smem_bytes(const SysGeom &g) {
 }
 
 cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
-                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st) {
+                        DofArrays dof, uint8_t *bins, int *err, cudaStream_t st, int g_first, int g_count) {
+    if (g_count < 0) g_count = g.D - g_first;
+    if (g_first < 0 || g_first + g_count > g.D) return cudaErrorInvalidValue;
+    if (g_count == 0) return cudaSuccess;
     const double pi = acos(-1.0);  // PARENT.cpp:112
     const double modfit_bs = (2 * pi + 0.000000005) / kModfitBins;  // PARENT.cpp:569
     const size_t smem = prep_smem_bytes(g);
     auto kern = double_prec ? prep_kernel<false> : prep_kernel<true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<g.D, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof, bins, err, modfit_bs, pi);
+    kern<<<g_count, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof, bins, err, modfit_bs,
+                                          pi, g_first);
     return cudaGetLastError();
 }
 
