@@ -84,6 +84,8 @@ struct Hist32Args {
     int *err;
     uint32_t *ovf_all;  // per CTA: [2 * words_per_lane][32] overflow counts (units of 32,768)
     int fc, nst, bmax;
+    uint32_t kw, kneg;  // 128 (bytes per counter word row) and -128 * 65536
+    uint32_t k64, kneg64, khalf;  // 64, -64, 65535 (16-bit layout)
 };
 
 // W32: 32-bit counters, word idx * 32 + lane, reduction value 1, no folding.
@@ -214,30 +216,46 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                             const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
                             const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
                             if (off + 16 <= fvalid) {
-                                // two frames per IMAD (idx < 2500 never carries into
-                                // the upper half); word idx >> 1 of this lane, half idx & 1
-                                uint32_t ix[8];
-#pragma unroll
-                                for (int q = 0; q < 4; q++) {
-                                    ix[2 * q] = __byte_perm(rw[q], 0u, 0x4140) * Bc + __byte_perm(cw[q], 0u, 0x4140);
-                                    ix[2 * q + 1] =
-                                        __byte_perm(rw[q], 0u, 0x4342) * Bc + __byte_perm(cw[q], 0u, 0x4342);
-                                }
-                                // frames in the order 0, 4, 8, 12, 1, 5, ...: consecutive
-                                // reductions of a lane are four frames apart, so runs of
-                                // one bin in correlated trajectories do not queue
-                                // read-modify-writes on one word back to back
-#pragma unroll
-                                for (int k = 0; k < 4; k++) {
+                                if (W32) {
+                                    // word addresses hbase + 128 idx for the 16 frames, with
+                                    // the multiplies on the FMA pipe (multipliers come from
+                                    // the launch arguments, so they stay IMADs): the ALU
+                                    // pipe is this loop's busiest unit
+                                    uint32_t ad[16];
 #pragma unroll
                                     for (int q = 0; q < 4; q++) {
-                                        const uint32_t v = ix[2 * q + (k >> 1)];
-                                        if (W32)
-                                            red_add1_nc(hbase + (((k & 1) ? (v >> 16) : (v & 0xffffu)) << 7));
-                                        else if (k & 1)
-                                            red_add_nc(hbase + ((v >> 17) << 7), ((v >> 16) & 1u) * 0xffffu + 1u);
-                                        else
-                                            red_add_nc(hbase + ((v & 0xfffeu) << 6), (v & 1u) * 0xffffu + 1u);
+#pragma unroll
+                                        for (int h = 0; h < 2; h++) {
+                                            const uint32_t sel = h ? 0x4342u : 0x4140u;
+                                            const uint32_t v = __byte_perm(rw[q], 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
+                                            const uint32_t hi = v >> 16;
+                                            ad[4 * q + 2 * h + 1] = hi * a.kw + hbase;
+                                            ad[4 * q + 2 * h] = v * a.kw + hbase + hi * a.kneg;
+                                        }
+                                    }
+                                    // frames 0, 4, 8, 12, 1, 5, ...
+#pragma unroll
+                                    for (int k = 0; k < 4; k++) {
+#pragma unroll
+                                        for (int q = 0; q < 4; q++) red_add1_nc(ad[4 * q + k]);
+                                    }
+                                } else {
+                                    // two frames per IMAD (idx < 2500 never carries into the
+                                    // upper half); word idx >> 1 of this lane, half idx & 1.
+                                    // The half's value (1 or 65536) and the second frame's
+                                    // address are formed with IMADs (runtime multipliers), the
+                                    // first frame's address on the ALU, to balance the two pipes
+#pragma unroll
+                                    for (int q = 0; q < 4; q++) {
+#pragma unroll
+                                        for (int h = 0; h < 2; h++) {
+                                            const uint32_t sel = h ? 0x4342u : 0x4140u;
+                                            const uint32_t v = __byte_perm(rw[q], 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
+                                            const uint32_t hi = v >> 16;
+                                            const uint32_t b0 = v & 1u, b1 = hi & 1u;
+                                            red_add_nc(hbase + ((v & 0xfffeu) << 6), b0 * a.khalf + 1u);
+                                            red_add_nc(hi * a.k64 + hbase + b1 * a.kneg64, b1 * a.khalf + 1u);
+                                        }
                                     }
                                 }
                             } else {  // ragged end of the trajectory
@@ -408,6 +426,11 @@ cudaError_t launch(Hist32Args &a, void *scratch, size_t scratch_bytes, cudaStrea
     cudaError_t e = wide_counters(a.bmax) ? cudaSuccess : cudaMemsetAsync(scratch, 0, need, st);
     if (e != cudaSuccess) return e;
     a.ovf_all = (uint32_t *)scratch;
+    a.kw = 128u;
+    a.kneg = 0u - (128u << 16);
+    a.k64 = 64u;
+    a.kneg64 = 0u - 64u;
+    a.khalf = 0xffffu;
     const size_t smem = smem_bytes(a.bmax, a.fc, a.nst);
     if (wide_counters(a.bmax)) {
         e = cudaFuncSetAttribute(pairs_hist32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
