@@ -56,6 +56,21 @@ METRIC = "DOF-pair x frame updates/s @50 bins (all-pairs 2D-histogram MI + MIST)
 UNIT = "updates/s"
 
 
+def traffic_per_update(slots: int):
+    """DRAM bytes per update of the pair kernel from the committed ncu capture
+    (profiles/), or None: the capture is on a smaller case (2,994 DOFs x 100k
+    frames) and is scaled by this launch's updates."""
+    name = ("pairs_hist32_kernel_precision_path_2994dof_100k_30bins.md" if slots == 32
+            else "pairs_hist_kernel_precision_path_2994dof_100k.md")
+    try:
+        for line in (ROOT / "profiles" / name).read_text().splitlines():
+            if line.startswith("dram_bytes_per_update:"):
+                return float(line.split(":")[1]), name
+    except OSError:
+        pass
+    return None, name
+
+
 def hist_slots(bins: int) -> int:
     """Pair slots per CTA of the histogram layout the library picks (32 with
     32-bit counters up to 35 bins, else 16; PG_HIST_SLOTS forces one)."""
@@ -489,10 +504,13 @@ def run_gb300(args):
     if form == "hist":
         red_peak = eng.probe_smem_red_rate()
         achieved = units / pair_s
+        bpu, prof = traffic_per_update(hist_slots(args.bins))
         roofline = {"bound": "smem", "achieved": achieved / 1e9, "peak": red_peak / 1e9, "unit": "Gred/s",
-                    "frac": achieved / red_peak, "traffic": None,
+                    "frac": achieved / red_peak, "traffic": bpu * units if bpu else None,
                     "note": "one shared-memory reduction per pair-frame update; peak = conflict-free "
-                            "red.shared rate measured live on this GPU (pg_probe_smem_red_rate)"}
+                            "red.shared rate measured live on this GPU (pg_probe_smem_red_rate); traffic = "
+                            "DRAM bytes per update of the ncu capture in profiles/" + prof + " x this launch's "
+                            "updates (bytes per launch)"}
     else:
         achieved = 2.0 * args.bins * args.bins * units / pair_s / 1e12
         peak = 2.0 * float(peaks.get("bf16_tflops", 1900.0))

@@ -491,15 +491,16 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
     return cudaGetLastError();
 }
 
-// Form choice, from measured GB300 pair-kernel times at 7,494 DOFs x 500,000
-// frames: the histogram form takes ~3.5 s at any bin count (bound by
-// shared-memory reductions, one per update); the one-hot form takes 2.1 s at
-// 10 bins, 8.1 s at 20 and 50 s at 50 (B1*B2 FP8 MACs per update, bound by
-// its one-hot tile build). Its time grows as B^2, so it wins up to ~12 bins.
+// Form choice, from measured GB300 pair-kernel times at 2,994 DOFs x 100,000
+// frames: the histogram form takes 85.5 ms at any bin count up to 32 (32-slot
+// layout, one conflict-free shared-memory reduction per update) and 117.6 ms
+// from 36 to 50 (16-slot layout); the one-hot form takes 45.9 / 58.5 / 71.3 /
+// 86.4 / 101.6 ms at 8 / 9 / 10 / 11 / 12 bins (B1*B2 FP8 MACs per update, so
+// its time grows as B^2). The one-hot form wins up to 10 bins.
 int autotune_form(const SysGeom &g) {
     int bmax = 0;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (pairs_onehot_supported(g) && bmax <= 12 && g.F >= 4096) return PG_FORM_ONEHOT;
+    if (pairs_onehot_supported(g) && bmax <= 10 && g.F >= 4096) return PG_FORM_ONEHOT;
     return PG_FORM_HIST;
 }
 
