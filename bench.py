@@ -56,6 +56,22 @@ METRIC = "DOF-pair x frame updates/s @50 bins (all-pairs 2D-histogram MI + MIST)
 UNIT = "updates/s"
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over all ranks (x itself without a process group): the
+    timed region of a multi-rank run is the slowest rank's."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(base: int, rank: int) -> int:
+    """Seed of a rank's own synthetic system: independent replicas, no shared data."""
+    return base + 7919 * rank
+
+
 def traffic_per_update(slots: int):
     """DRAM bytes per update of the pair kernel from the committed ncu capture
     (profiles/), or None: the capture is on a smaller case (2,994 DOFs x 100k
@@ -234,7 +250,7 @@ def run_batch(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     bins = (args.bins,) * 6
-    systems = batch_systems(seed=64 + rank)
+    systems = batch_systems(seed=replica_seed(64, rank))
     es = 4
     eng = pg.Engine(local)
     sizes = [(3 * a - 6) * f * es for a, f, _, _ in systems]
@@ -247,7 +263,7 @@ def run_batch(args):
         nb, na = nd + 2, nd + 1
         p = dbuf + off
         ptrs = (p, p + nb * f * es, p + (nb + na) * f * es)
-        eng.synth_device(a, f, 0, ptrs, f, seed=sd + 7919 * rank, n_latents=lat, frac_bimodal_dih=0.0,
+        eng.synth_device(a, f, 0, ptrs, f, seed=replica_seed(sd, rank), n_latents=lat, frac_bimodal_dih=0.0,
                          frac_bimodal_bond=0.0)
         views.append(pg.BatView(nd, f, 0, 1, f, *ptrs))
         D = 3 * a - 6
@@ -278,10 +294,7 @@ def run_batch(args):
         eng.synchronize()
         torch.cuda.synchronize(local)
         ms = ev0.elapsed_time(ev1)
-        if dist:
-            tt = torch.tensor([ms], device=f"cuda:{local}")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = max_over_ranks(ms, dist, f"cuda:{local}")
         return ms / steps
 
     for _ in range(args.warmup):
@@ -327,10 +340,7 @@ def run_batch(args):
         for _ in range(args.e2e_steps):
             eng.entropy_batch(hviews, bins, args.form, bodies=bodies, trees=True)
         sec = (time.perf_counter() - t0) / args.e2e_steps
-        if dist:
-            tt = torch.tensor([sec], device=f"cuda:{local}")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            sec = float(tt.item())
+        sec = max_over_ranks(sec, dist, f"cuda:{local}")
         n_edges = sum(3 * v.n_dihedrals + 2 for v in views)
         e2e = {"value": units * world / sec, "unit": UNIT, "h2d_bytes_per_step": total_bytes,
                "d2h_bytes_per_step": sum(body_elems) * 8 + n_edges * 32 + 80 * len(views),
@@ -401,7 +411,7 @@ def run_gb300(args):
     nb, na, nd = n_dih + 2, n_dih + 1, n_dih
     dbuf = eng.alloc(D * F * es)
     ptrs = (dbuf, dbuf + nb * F * es, dbuf + (nb + na) * F * es)
-    eng.synth_device(n_atoms, F, prec, ptrs, F, seed=20260 + rank, n_latents=lat,
+    eng.synth_device(n_atoms, F, prec, ptrs, F, seed=replica_seed(20260, rank), n_latents=lat,
                      frac_bimodal_dih=fbd, frac_bimodal_bond=fbb)
     view = pg.BatView(n_dih, F, prec, 1, F, *ptrs)
     stream = torch.cuda.ExternalStream(eng.stream(), device=torch.device("cuda", local))
@@ -434,10 +444,8 @@ def run_gb300(args):
     eng.synchronize()
     torch.cuda.synchronize(local)
     ms_total = ev0.elapsed_time(ev1)
+    ms_total = max_over_ranks(ms_total, dist, f"cuda:{local}")
     if dist:
-        tt = torch.tensor([ms_total], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
         dist.barrier()
     clk = clocks.stop()
     launches = eng.launch_count() - launches0
@@ -484,10 +492,7 @@ def run_gb300(args):
                           "entropy_device_ms": float(te[4]), "mist_ms": float(tm[2])})
         t1 = time.perf_counter()
         sec = (t1 - t0) / args.e2e_steps
-        if dist:
-            tt = torch.tensor([sec], device=f"cuda:{local}")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            sec = float(tt.item())
+        sec = max_over_ranks(sec, dist, f"cuda:{local}")
         e2e = {"value": units * world / sec, "unit": UNIT, "h2d_bytes_per_step": D * F * es,
                "d2h_bytes_per_step": total * 8 + (D - 1) * (4 * 4 + 8 + 8), "ms_per_step": sec * 1e3,
                "breakdown": parts[-1]}
