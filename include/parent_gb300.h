@@ -148,6 +148,22 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
 PG_API int pg_mist_noalloc(int n_dihedrals, const double *mi, double *edge_mi, int *edge_from,
                            int *edge_to, void *stream);
 
+/* One shard of the pair work of one trajectory, for splitting a system over
+ * several GPUs (the reference splits DOF blocks over MPI ranks,
+ * PARENT.cpp:333-414, 775-1119). The histogram form's tile list is cut into
+ * n_shards contiguous ranges of equal tile count; every shard preprocesses all
+ * DOFs, computes the 2D entropies of its own pairs and writes them into `out`
+ * (.par body layout) with zeros everywhere else; shard 0 also writes the 1D
+ * entropies. The element-wise sum of the n_shards bodies (any order: every
+ * entry is non-zero in at most one shard, so the FP64 sum is exact) is the
+ * pg_entropy body. MIST then runs on the merged body (pg_mist with body). */
+PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form, int shard,
+                            int n_shards, pg_par_body *out);
+/* Which .par body entries shard `shard` of `n_shards` writes (1) for a system
+ * of n_dihedrals and these bin counts: mask[total body length], body order.
+ * Host only; no context or GPU needed. */
+PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_shards, uint8_t *mask);
+
 /* Many independent trajectories in one run (no reference counterpart: the
  * reference handles one trajectory per PARENT.x / get_PAR_MIST.x process).
  * Every system gets the PARENT.x computation and its MIST tree; the pair

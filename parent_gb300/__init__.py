@@ -82,6 +82,8 @@ def lib() -> C.CDLL:
         "pg_mist": (i, [vp, i, C.POINTER(ParBodyC), C.POINTER(MistEdge), dp]),
         "pg_entropy_batch": (i, [vp, i, C.POINTER(BatView), C.POINTER(C.c_int), i, C.POINTER(ParBodyC),
                                  C.POINTER(C.POINTER(MistEdge)), dp]),
+        "pg_entropy_shard": (i, [vp, C.POINTER(BatView), C.POINTER(C.c_int), i, i, i, C.POINTER(ParBodyC)]),
+        "pg_shard_mask": (i, [i, C.POINTER(C.c_int), i, i, C.POINTER(C.c_uint8)]),
         "pg_last_timings": (i, [vp, dp]),
         "pg_launch_count": (i64, [vp]),
         "pg_last_form": (i, [vp]),
@@ -300,6 +302,18 @@ class Engine:
                                     ("left", "i4")])
                 res.append((a, totals[10 * k:10 * k + 10].copy()))
         return outs, res
+
+    def entropy_shard(self, traj: Trajectory | BatView, bins, shard: int, n_shards: int,
+                      form: str | int = "auto") -> ParBody:
+        """Shard `shard` of `n_shards` of PARENT.x (pg_entropy_shard): this shard's
+        2D entropies (and, for shard 0, the 1D entropies), zeros elsewhere."""
+        v = traj if isinstance(traj, BatView) else traj.view()
+        b = (C.c_int * 6)(*bins)
+        f = FORMS[form] if isinstance(form, str) else int(form)
+        out = ParBody.empty(v.n_dihedrals)
+        body = out.c()
+        _check(lib().pg_entropy_shard(self._ctx, C.byref(v), b, f, shard, n_shards, C.byref(body)), self._ctx)
+        return out
 
     def pair_counts(self, traj: Trajectory, bins, pairs, form: str = "hist") -> list[np.ndarray]:
         """Raw 2D histograms of explicit (g1 < g2) pairs from the GPU pair kernel."""

@@ -328,6 +328,21 @@ static int run_hist32(pg_ctx *ctx, const SysGeom &g, const DofArrays &dof, const
 static int mist_edges_to_user(pg_ctx *ctx, int n_dihedrals, const double *hmi, const int *hf, const int *ht,
                               const double *s1, pg_mist_edge *edges, double totals[10]);
 
+// Tile list of the histogram layout a geometry uses, and the contiguous range
+// [b, e) of it that shard `shard` of `n_shards` owns (balanced by tile count;
+// tiles carry equal work apart from the diagonal and ragged edges).
+static std::vector<PairTile> layout_tiles(const SysGeom &g, int *T_out) {
+    int T = 0, fc = 0, nst = 0;
+    const bool h32 = use_hist32(g);
+    if (!h32 && !pairs_hist_config(bmax_of(g), &T, &fc, &nst)) return {};
+    *T_out = h32 ? 32 : T;
+    return h32 ? build_tiles32(g.D) : build_tiles(g.D, T);
+}
+static void shard_range(int64_t n, int shard, int n_shards, int64_t *b, int64_t *e) {
+    *b = n * shard / n_shards;
+    *e = n * (shard + 1) / n_shards;
+}
+
 // Entropies of a HOST trajectory with the upload overlapped: the DOFs are
 // split into up to 16 groups on column super-block boundaries of the tile
 // list; a second stream uploads group after group, and on the context's
@@ -600,6 +615,103 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     ctx->timings[4] = ms[0] + ms[1] + ms[2] + ms[3];
     if (rc) return rc;
     ctx->resident = true;
+    return PG_OK;
+}
+
+PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_shards, uint8_t *mask) {
+    if (n_dihedrals < 0 || !bins || !mask || n_shards < 1 || shard < 0 || shard >= n_shards)
+        return fail(nullptr, PG_ERR_ARG, "invalid shard arguments");
+    SysGeom g{};
+    g.n_dih = n_dihedrals;
+    g.nb = n_dihedrals + 2;
+    g.na = n_dihedrals + 1;
+    g.nd = n_dihedrals;
+    g.D = g.nb + g.na + g.nd;
+    for (int k = 0; k < 6; k++) {
+        if (bins[k] < 1 || (k >= 3 && bins[k] > PG_MAX_BINS_2D)) return fail(nullptr, PG_ERR_ARG, "bad bin count");
+        g.bins[k] = bins[k];
+    }
+    int T = 0;
+    const std::vector<PairTile> tl = layout_tiles(g, &T);
+    const ParLayout L = par_layout(g.n_dih);
+    memset(mask, 0, (size_t)L.total);
+    if (shard == 0) memset(mask, 1, (size_t)g.D);  // the 1D entropies (body offsets 0 .. D-1)
+    int64_t b = 0, e = 0;
+    shard_range((int64_t)tl.size(), shard, n_shards, &b, &e);
+    for (int64_t k = b; k < e; k++) {
+        const PairTile &t = tl[k];
+        for (int r = 0; r < t.nrow; r++)
+            for (int c = 0; c < t.ncol; c++) {
+                const int g1 = t.row0 + r, g2 = t.col0 + c;
+                if (g1 < g2) mask[par_pair_index(L, g.nb, g.na, g.nd, g1, g2)] = 1;
+            }
+    }
+    return PG_OK;
+}
+
+PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form, int shard,
+                            int n_shards, pg_par_body *out) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (n_shards < 1 || shard < 0 || shard >= n_shards) return fail(ctx, PG_ERR_ARG, "shard %d of %d", shard, n_shards);
+    if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "shards use the histogram form");
+    if (form != PG_FORM_AUTO && form != PG_FORM_HIST) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    int rc = run_prep(ctx, traj, bins);  // every shard bins all D columns (O(D F))
+    if (rc) return rc;
+    const SysGeom &g = ctx->geo;
+    cudaStream_t st = ctx->stream;
+    const ParLayout L = par_layout(g.n_dih);
+    CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
+    CK(cudaMemsetAsync(ctx->par.p, 0, (size_t)L.total * sizeof(double), st));
+    DofArrays dof = dof_arrays(ctx, g.D);
+    if (shard == 0)
+        CK(cudaMemcpyAsync((double *)ctx->par.p + L.s1b, dof.s1, (size_t)g.D * sizeof(double),
+                           cudaMemcpyDeviceToDevice, st));
+    int T = 0;
+    const std::vector<PairTile> tl = layout_tiles(g, &T);
+    if (tl.empty() && g.D > 1) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
+    int64_t b = 0, e = 0;
+    shard_range((int64_t)tl.size(), shard, n_shards, &b, &e);
+    PairOut po;
+    po.par = (double *)ctx->par.p;
+    po.mi = nullptr;  // a shard's MI matrix is partial: MIST runs on the merged body
+    po.L = L;
+    po.counts = nullptr;
+    po.counts_bmax = 0;
+    if (e > b) {
+        DevBuf tbuf;
+        CK(tbuf.ensure(sizeof(PairTile) * (size_t)(e - b)));
+        CK(cudaMemcpyAsync(tbuf.p, tl.data() + b, sizeof(PairTile) * (size_t)(e - b), cudaMemcpyHostToDevice, st));
+        rc = ensure_fix_table(ctx, g.F);
+        if (rc) return rc;
+        if (T == 32) {
+            const size_t sb = pairs_hist32_scratch_bytes(bmax_of(g), pairs_hist32_grid(e - b));
+            CK(ctx->scratch.ensure(sb));
+            CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                                   ctx->nfix_scale, (const PairTile *)tbuf.p, e - b, po, (int *)ctx->errw.p,
+                                   ctx->scratch.p, sb, st));
+        } else {
+            CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
+                                 ctx->nfix_scale, (const PairTile *)tbuf.p, e - b, T, po, (int *)ctx->errw.p, st));
+        }
+        ctx->launches++;
+        CK(cudaStreamSynchronize(st));  // the private tile buffer is released on return
+    }
+    if (out) {
+        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
+        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
+        for (int k = 0; k < 9; k++) {
+            const int64_t n = off[k + 1] - off[k];
+            if (n <= 0) continue;
+            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
+            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+        }
+    }
+    rc = check_err_words(ctx);
+    if (rc) return rc;
+    ctx->last_form = PG_FORM_HIST;
+    ctx->resident = false;
     return PG_OK;
 }
 

@@ -1,0 +1,125 @@
+"""Splitting one trajectory's pair work over ranks (pg_entropy_shard).
+
+CPU: the shards' body masks partition the .par body, and two gloo ranks that
+each hold their shard of a body (the oracle's values on the rank's own
+entries, zeros elsewhere) reproduce the whole body exactly with the SUM
+reduction the driver uses. GPU: shard bodies from the CUDA path sum to the
+pg_entropy body bit for bit, and each shard writes only its own entries."""
+from __future__ import annotations
+
+import multiprocessing as mp
+import socket
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import parent_gb300 as pg
+import parent_gb300.shard as sh
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("n_dih,bins,n_shards", [(20, (50,) * 6, 3), (20, (30,) * 6, 2), (3, (50,) * 6, 7),
+                                                  (0, (50,) * 6, 2), (60, (10, 20, 30, 100, 40, 20), 4),
+                                                  (40, (50,) * 6, 1)])
+def test_shard_masks_partition_the_body(n_dih, bins, n_shards):
+    masks = [sh.shard_mask(n_dih, bins, s, n_shards) for s in range(n_shards)]
+    owners = np.sum([m.astype(int) for m in masks], axis=0)
+    assert owners.size == sum(pg.block_sizes(n_dih).values())
+    assert owners.min() == 1 and owners.max() == 1
+    D = 3 * n_dih + 3
+    assert masks[0][:D].all()  # shard 0 owns the 1D entropies
+    if n_shards > 1 and n_dih >= 20:  # pair entries are spread evenly
+        sizes = [int(m[D:].sum()) for m in masks]
+        assert max(sizes) <= 1.6 * (sum(sizes) / n_shards)
+
+
+def test_shard_mask_rejects_bad_arguments():
+    with pytest.raises(pg.PGError):
+        sh.shard_mask(5, (50,) * 6, 2, 2)
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, n_dih, bins, full, q):
+    try:
+        sys.path.insert(0, str(ROOT))
+        import torch.distributed as dist
+
+        import parent_gb300.shard as shm
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+        local = np.where(shm.shard_mask(n_dih, bins, rank, world), full, 0.0)
+        merged = shm.merge_bodies(n_dih, local, dist, "cpu")
+        dist.destroy_process_group()
+        q.put((rank, None if merged is None else merged.flat(), None))
+    except Exception as e:
+        q.put((rank, None, repr(e)))
+
+
+def test_two_gloo_ranks_merge_shards_exactly():
+    pytest.importorskip("torch.distributed")
+    n_dih, bins = 15, (50,) * 6
+    t = pg.synth_host(n_dih + 3, 4000, double_prec=1, seed=3, frac_bimodal_dih=0.2)
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    full = np.concatenate([ref[k] for k in pg.block_sizes(n_dih)])
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, n_dih, bins, full, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    try:
+        for _ in range(2):
+            r = q.get(timeout=180)
+            res[r[0]] = r
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.kill()
+    assert res[0][2] is None and res[1][2] is None, (res[0][2], res[1][2])
+    assert res[1][1] is None
+    assert np.array_equal(res[0][1].view(np.uint64), full.view(np.uint64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_atoms,F,bins,n_shards", [(60, 20000, (50,) * 6, 3), (40, 9000, (30,) * 6, 2),
+                                                       (25, 5000, (50, 50, 50, 100, 100, 100), 4)])
+def test_gpu_shards_sum_to_the_whole(n_atoms, F, bins, n_shards):
+    t = pg.synth_host(n_atoms, F, double_prec=0, seed=n_atoms, frac_bimodal_dih=0.2)
+    n = n_atoms - 3
+    with pg.Engine(0) as eng:
+        whole = eng.entropy(t, bins, "hist").flat()
+        acc = np.zeros_like(whole)
+        for s in range(n_shards):
+            part = eng.entropy_shard(t, bins, s, n_shards).flat()
+            mask = sh.shard_mask(n, bins, s, n_shards)
+            assert not np.any(part[~mask]), s
+            acc += part
+        assert np.array_equal(acc.view(np.uint64), whole.view(np.uint64))
+        merged = sh.entropy_sharded(eng, t, bins)  # one rank: the whole body
+        assert np.array_equal(merged.flat().view(np.uint64), whole.view(np.uint64))
+        e1, t1 = eng.mist(n, merged)
+        eng.entropy(t, bins, "hist")
+        e2, t2 = eng.mist(n)
+        assert np.array_equal(e1, e2) and np.array_equal(t1, t2)
+
+
+@pytest.mark.gpu
+def test_gpu_shard_rejects_onehot_and_bad_index():
+    t = pg.synth_host(10, 2000, double_prec=0, seed=1)
+    with pg.Engine(0) as eng:
+        with pytest.raises(pg.PGError) as ex:
+            eng.entropy_shard(t, (50,) * 6, 0, 2, form="onehot")
+        assert ex.value.code == pg.PG_ERR_UNSUPPORTED
+        with pytest.raises(pg.PGError) as ex:
+            eng.entropy_shard(t, (50,) * 6, 2, 2)
+        assert ex.value.code == pg.PG_ERR_ARG
