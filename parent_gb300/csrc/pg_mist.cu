@@ -12,8 +12,16 @@
 //             to a fixed v.
 // The step winner is the Out vertex with the largest key, ties broken by
 // (type(from), type(v), position(from), v) ascending, i.e. the reference's
-// scan order. One persistent CTA of 1024 threads keeps key/from in shared
-// memory and reads one MI row (the vertex that just joined) per step.
+// scan order.
+//
+// One persistent CTA; thread t owns the vertices v = t, t + blockDim, ... and
+// is the only thread that touches their key/from, so a step is one pass over
+// the owned vertices (read the MI row of the vertex that joined last, relax,
+// keep the best candidate), a warp reduction, ONE block barrier, and a
+// redundant reduction of the per-warp bests by every warp (per-warp bests are
+// double-buffered by step parity). The position of the vertex that joined in
+// the previous step is taken from registers, every older one from shared
+// memory (written before the last barrier).
 //
 // MI values are compared as order-preserving 64-bit integer images of the
 // doubles (sign-magnitude flipped to two's-complement order, -0 folded onto
@@ -28,17 +36,14 @@ namespace pg {
 
 namespace {
 
-constexpr int kThreads = 1024;
-constexpr int kWarps = kThreads / 32;
+constexpr int kMaxThreads = 1024;
+constexpr int kMaxWarps = kMaxThreads / 32;
 
-struct Cand {
-    unsigned long long key;
-    int v;  // -1: none
-};
-
-// order-preserving image of a (non-NaN) double; 0 is below every value
+// order-preserving image of a double; 0 is below every value. NaN maps to 0:
+// it never beats anything, as no strict '>' with a NaN holds in the reference.
 __device__ __forceinline__ unsigned long long okey(double x) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return 0ull;  // NaN
     if (b == 0x8000000000000000ull) b = 0ull;  // -0 == +0
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
@@ -47,105 +52,119 @@ __device__ __forceinline__ double okey_value(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
-__device__ __forceinline__ int type_of(int g, int nb, int na) { return dof_type(g, nb, na); }
+// A candidate: its key and a secondary word that orders equal keys,
+// ~((type(from) << 62) | (type(v) << 60) | (pos(from) << 30) | v), so that the
+// reference's first-in-scan-order candidate has the LARGEST (key, sec).
+struct Cand {
+    unsigned long long key, sec;
+    int v, from;
+};
 
-// true if candidate a comes before candidate b in the reference's order
-__device__ __forceinline__ bool better(const Cand &a, const Cand &b, const int *from,
-                                       const int *pos, int nb, int na) {
-    if (a.v < 0) return false;
-    if (b.v < 0) return true;
-    if (a.key > b.key) return true;
-    if (a.key < b.key) return false;
-    const int fa = from[a.v], fb = from[b.v];
-    const int tfa = fa >= 0 ? type_of(fa, nb, na) : 3, tfb = fb >= 0 ? type_of(fb, nb, na) : 3;
-    if (tfa != tfb) return tfa < tfb;
-    const int tva = type_of(a.v, nb, na), tvb = type_of(b.v, nb, na);
-    if (tva != tvb) return tva < tvb;
-    const int pa = fa >= 0 ? pos[fa] : 0x7fffffff, pb = fb >= 0 ? pos[fb] : 0x7fffffff;
-    if (pa != pb) return pa < pb;
-    return a.v < b.v;
+__device__ __forceinline__ bool beats(const Cand &a, const Cand &b) {
+    return a.key > b.key || (a.key == b.key && a.sec > b.sec);
+}
+
+__device__ __forceinline__ unsigned long long sec_of(int tf, int tv, int posf, int v) {
+    return ~(((unsigned long long)tf << 62) | ((unsigned long long)tv << 60) |
+             ((unsigned long long)(unsigned)posf << 30) | (unsigned long long)(unsigned)v);
+}
+
+__device__ __forceinline__ Cand shfl_cand(const Cand &c, int o) {
+    Cand r;
+    r.key = __shfl_xor_sync(0xffffffffu, c.key, o);
+    r.sec = __shfl_xor_sync(0xffffffffu, c.sec, o);
+    r.v = __shfl_xor_sync(0xffffffffu, c.v, o);
+    r.from = __shfl_xor_sync(0xffffffffu, c.from, o);
+    return r;
+}
+
+__device__ __forceinline__ Cand warp_best(Cand c) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const Cand other = shfl_cand(c, o);
+        if (beats(other, c)) c = other;
+    }
+    return c;
 }
 
 template <bool SMEM>
 __device__ __forceinline__ void mist_body(int D, int nb, int na, const double *__restrict__ mi,
-                                          unsigned long long *gkey, int *gfrom, int *pos, double *edge_mi,
+                                          unsigned long long *gkey, int *gfrom, int *gpos, double *edge_mi,
                                           int *edge_from, int *edge_to) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned long long *key = SMEM ? (unsigned long long *)smem : gkey;
     int *from = SMEM ? (int *)(smem + (size_t)D * sizeof(unsigned long long)) : gfrom;
-    __shared__ Cand wbest[kWarps];
-    __shared__ int s_win;
+    int *pos = SMEM ? from + D : gpos;
+    __shared__ Cand wbest[2][kMaxWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthr = blockDim.x, nwarps = nthr >> 5;
 
     // In = {bond 0} (get_PAR_MIST.cpp:419-422)
-    for (int v = tid; v < D; v += kThreads) {
+    for (int v = tid; v < D; v += nthr) {
         key[v] = 0ull;
         from[v] = v == 0 ? -2 : -1;  // -2: in the tree, -1: no In partner yet
     }
-    if (tid == 0) {
-        pos[0] = 0;
-        s_win = 0;
-    }
+    if (tid == 0) pos[0] = 0;
+    int last_w = 0, last_pos = 0;  // the vertex that joined last and its position
+    // ordering (and the initial pos) only need this barrier once: afterwards
+    // every thread touches only its own vertices' key/from
     __syncthreads();
 
-    for (int step = 0; step < D; step++) {
-        // relax keys with the row of the vertex that joined last
-        const int w = s_win;
-        const int tw = type_of(w, nb, na);
-        const double *row = mi + (int64_t)w * D;
-        for (int v = tid; v < D; v += kThreads) {
-            const int f = from[v];
+    for (int step = 0; step < D - 1; step++) {
+        const int tw = dof_type(last_w, nb, na);
+        const double *row = mi + (int64_t)last_w * D;
+        Cand best{0ull, 0ull, -1, -1};
+        for (int v0 = tid; v0 < D; v0 += 4 * nthr) {
+            // the row loads of up to four owned vertices go out together
+            double mv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int v = v0 + u * nthr;
+                mv[u] = v < D ? __ldg(row + v) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+            const int v = v0 + u * nthr;
+            if (v >= D) break;
+            int f = from[v];
             if (f == -2) continue;
-            const unsigned long long m = okey(__ldg(row + v));
-            const unsigned long long k = key[v];
-            if (m > k || (m == k && f >= 0 && tw < type_of(f, nb, na))) {
+            const unsigned long long m = okey(mv[u]);
+            unsigned long long k = key[v];
+            if (m > k || (m == k && f >= 0 && tw < dof_type(f, nb, na))) {
                 key[v] = m;
-                from[v] = w;
+                from[v] = last_w;
+                k = m;
+                f = last_w;
+            }
+            const int tf = f >= 0 ? dof_type(f, nb, na) : 3;
+            const int pf = f < 0 ? (1 << 30) - 1 : (f == last_w ? last_pos : pos[f]);
+            const Cand c{k, sec_of(tf, dof_type(v, nb, na), pf, v), v, f};
+            if (best.v < 0 || beats(c, best)) best = c;
             }
         }
-        if (step == D - 1) break;
+        best = warp_best(best);
+        if (lane == 0) wbest[step & 1][warp] = best;
         __syncthreads();
-        // argmax in the reference's order
-        Cand best{0ull, -1};
-        for (int v = tid; v < D; v += kThreads) {
-            if (from[v] == -2) continue;
-            const Cand c{key[v], v};
-            if (better(c, best, from, pos, nb, na)) best = c;
+        // every warp reduces the per-warp bests (the same data, the same result)
+        Cand b = lane < nwarps ? wbest[step & 1][lane] : Cand{0ull, 0ull, -1, -1};
+        if (b.v < 0) b.key = 0ull, b.sec = 0ull;
+        b = warp_best(b);
+        const int w = b.v < 0 ? 0 : b.v;
+        if (tid == 0) {
+            edge_mi[step] = okey_value(b.key);
+            edge_from[step] = b.v < 0 ? -1 : b.from;
+            edge_to[step] = b.v;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            Cand other;
-            other.key = __shfl_xor_sync(0xffffffffu, best.key, o);
-            other.v = __shfl_xor_sync(0xffffffffu, best.v, o);
-            if (better(other, best, from, pos, nb, na)) best = other;
+        if (b.v >= 0 && w % nthr == tid) {  // the owner of the joining vertex
+            from[w] = -2;
+            pos[w] = step + 1;
         }
-        if (lane == 0) wbest[warp] = best;
-        __syncthreads();
-        if (warp == 0) {
-            Cand b = wbest[lane];
-            for (int o = 16; o > 0; o >>= 1) {
-                Cand other;
-                other.key = __shfl_xor_sync(0xffffffffu, b.key, o);
-                other.v = __shfl_xor_sync(0xffffffffu, b.v, o);
-                if (better(other, b, from, pos, nb, na)) b = other;
-            }
-            if (lane == 0) {
-                const int v = b.v < 0 ? 0 : b.v;
-                edge_mi[step] = okey_value(b.key);
-                edge_from[step] = b.v < 0 ? -1 : from[v];
-                edge_to[step] = b.v;
-                if (b.v >= 0) {
-                    pos[v] = step + 1;
-                    from[v] = -2;
-                }
-                s_win = v;
-            }
-        }
-        __syncthreads();
+        last_w = w;
+        last_pos = step + 1;
     }
 }
 
 template <bool SMEM>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kMaxThreads, 1)
 mist_kernel(int D, int nb, int na, const double *__restrict__ mi, unsigned long long *gkey, int *gfrom,
             int *pos, double *edge_mi, int *edge_from, int *edge_to) {
     mist_body<SMEM>(D, nb, na, mi, gkey, gfrom, pos, edge_mi, edge_from, edge_to);
@@ -153,12 +172,19 @@ mist_kernel(int D, int nb, int na, const double *__restrict__ mi, unsigned long 
 
 // One CTA per system of a batch.
 template <bool SMEM>
-__global__ void __launch_bounds__(kThreads, 1) mist_batch_kernel(const MistDesc *__restrict__ sys) {
+__global__ void __launch_bounds__(kMaxThreads, 1) mist_batch_kernel(const MistDesc *__restrict__ sys) {
     const MistDesc &d = sys[blockIdx.x];
     unsigned long long *gkey = (unsigned long long *)d.scratch;
     int *gfrom = (int *)(gkey + d.D);
     int *pos = gfrom + d.D;
     mist_body<SMEM>(d.D, d.nb, d.na, d.mi, gkey, gfrom, pos, d.edge_mi, d.edge_from, d.edge_to);
+}
+
+// Threads per CTA for D vertices: one vertex per thread up to 1,024 (whole
+// warps, at least 64), 1,024 threads above.
+int mist_threads(int D) {
+    int t = (D + 31) / 32 * 32;
+    return t < 64 ? 64 : (t > kMaxThreads ? kMaxThreads : t);
 }
 
 // Dense symmetric MI matrix from a .par body on the device, get_mutual
@@ -187,30 +213,30 @@ cudaError_t launch_mist_impl(int D, int nb, int na, const double *mi, void *scra
     unsigned long long *gkey = (unsigned long long *)scratch;
     int *gfrom = (int *)(gkey + D);
     int *pos = gfrom + D;
-    const size_t smem = (size_t)D * (sizeof(unsigned long long) + sizeof(int));
+    const size_t smem = (size_t)D * (sizeof(unsigned long long) + 2 * sizeof(int));
+    const int nthr = mist_threads(D);
     if (smem <= 200 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(mist_kernel<true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        mist_kernel<true><<<1, kThreads, smem, st>>>(D, nb, na, mi, gkey, gfrom, pos, edge_mi,
-                                                     edge_from, edge_to);
+        mist_kernel<true><<<1, nthr, smem, st>>>(D, nb, na, mi, gkey, gfrom, pos, edge_mi, edge_from, edge_to);
     } else {
-        mist_kernel<false><<<1, kThreads, 0, st>>>(D, nb, na, mi, gkey, gfrom, pos, edge_mi,
-                                                   edge_from, edge_to);
+        mist_kernel<false><<<1, nthr, 0, st>>>(D, nb, na, mi, gkey, gfrom, pos, edge_mi, edge_from, edge_to);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_mist_batch(const MistDesc *sys, int n_sys, int max_D, cudaStream_t st) {
     if (n_sys <= 0) return cudaSuccess;
-    const size_t smem = (size_t)max_D * (sizeof(double) + sizeof(int));
+    const size_t smem = (size_t)max_D * (sizeof(unsigned long long) + 2 * sizeof(int));
+    const int nthr = mist_threads(max_D);
     if (smem <= 200 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(mist_batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        mist_batch_kernel<true><<<n_sys, kThreads, smem, st>>>(sys);
+        mist_batch_kernel<true><<<n_sys, nthr, smem, st>>>(sys);
     } else {
-        mist_batch_kernel<false><<<n_sys, kThreads, 0, st>>>(sys);
+        mist_batch_kernel<false><<<n_sys, nthr, 0, st>>>(sys);
     }
     return cudaGetLastError();
 }
