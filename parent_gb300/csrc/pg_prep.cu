@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
                                                         const void *ca, const void *cd,
                                                         int64_t ld, int prec, DofArrays dof,
                                                         uint8_t *bins, int *err,
-                                                        double modfit_bs, double pi, int g_first) {
+                                                        double modfit_bs, double pi, int g_first,
+                                                        int h1_copies) {
     extern __shared__ unsigned int sh[];
     const int g = g_first + blockIdx.x;
     const int type = dof_type(g, geo.nb, geo.na);
@@ -96,7 +97,8 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     // shared layout: [kWarps][kModfitBins] | [kWarps][B1] | [kWarps][B2] | scalars
     unsigned int *hmod = sh;
     unsigned int *h1 = hmod + kWarps * kModfitBins;
-    unsigned int *h2 = h1 + kWarps * B1;
+    unsigned int *h2 = h1 + h1_copies * B1;  // per-warp 1D histograms, or one shared copy for large B1
+    const int w1 = h1_copies > 1 ? warp : 0;
     __shared__ double s_shift, s_mn, s_mx;
     __shared__ double red_mn[kWarps], red_mx[kWarps];
     __shared__ float red_rmax[kWarps][kRegions], red_rmin[kWarps][kRegions];
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
         dof.shift[g] = modfit;
         dof.b2[g] = B2;
     }
-    for (int k = tid; k < kWarps * (B1 + B2); k += kThreads) h1[k] = 0;
+    for (int k = tid; k < h1_copies * B1 + kWarps * B2; k += kThreads) h1[k] = 0;
     __syncthreads();
 
     // ---- binning (PARENT.cpp:654-656 1D; :800-803 and the other 2D fills)
@@ -303,7 +305,7 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
             }
             if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
-            atomicAdd(&h1[warp * B1 + i1], 1u);
+            atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
             brow[f] = (uint8_t)i2;
         }
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
             int i2 = bin_index(x, mn, bs2);
             if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
-            atomicAdd(&h1[warp * B1 + i1], 1u);
+            atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
             brow[f] = (uint8_t)i2;
         }
@@ -325,8 +327,9 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     for (int k = tid; k < B1 + B2; k += kThreads) {
         unsigned int *h = k < B1 ? h1 : h2;
         const int kk = k < B1 ? k : k - B1, stride = k < B1 ? B1 : B2;
+        const int copies = k < B1 ? h1_copies : kWarps;
         unsigned int s = 0;
-        for (int w = 0; w < kWarps; w++) s += h[w * stride + kk];
+        for (int w = 0; w < copies; w++) s += h[w * stride + kk];
         h[kk] = s;
     }
     __syncthreads();
@@ -416,13 +419,23 @@ cudaError_t launch_nlogn_table(double *nlogn, int nmax, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-size_t prep_smem_bytes(const SysGeom &g) {
+// Per-warp private 1D histograms where they fit in 200 KB with the others,
+// one shared copy otherwise (up to 16,384 1D bins).
+static int prep_h1_copies(const SysGeom &g, int *m1_out, int *m2_out) {
     int m1 = 0, m2 = 0;
     for (int t = 0; t < 3; t++) {
         if (g.bins[t] > m1) m1 = g.bins[t];
         if (g.bins[3 + t] > m2) m2 = g.bins[3 + t];
     }
-    return (size_t)kWarps * (kModfitBins + m1 + m2) * sizeof(unsigned int);
+    *m1_out = m1;
+    *m2_out = m2;
+    return (size_t)kWarps * (kModfitBins + m1 + m2) * sizeof(unsigned int) <= 200 * 1024 ? kWarps : 1;
+}
+
+size_t prep_smem_bytes(const SysGeom &g) {
+    int m1 = 0, m2 = 0;
+    const int c1 = prep_h1_copies(g, &m1, &m2);
+    return ((size_t)kWarps * (kModfitBins + m2) + (size_t)c1 * m1) * sizeof(unsigned int);
 }
 
 cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
@@ -436,8 +449,10 @@ cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld,
     auto kern = double_prec ? prep_kernel<false> : prep_kernel<true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    int m1 = 0, m2 = 0;
+    const int c1 = prep_h1_copies(g, &m1, &m2);
     kern<<<g_count, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof, bins, err, modfit_bs,
-                                          pi, g_first);
+                                          pi, g_first, c1);
     return cudaGetLastError();
 }
 

@@ -472,3 +472,26 @@ def test_peaked_counts_above_16_bits(eng, monkeypatch, slots):
     body = eng.entropy(t, (50,) * 6, "hist")
     ref = oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6)
     compare_bodies(n_dih, body, ref)
+
+
+@pytest.mark.parametrize("bins", [(16384, 16384, 16384, 218, 218, 218), (16384, 7, 1, 218, 1, 50)])
+def test_maximum_bin_counts_match_oracle(eng, bins):
+    """The largest bin counts the ABI accepts: 16,384 1D bins and 218 2D bins
+    (the 1 x 1 tile layout), next to single-bin types."""
+    t = _synth_case(6, 6000, 0, seed=8, frac_bimodal_dih=0.2)
+    body = eng.entropy(t, bins, "hist")
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    compare_bodies(3, body, ref)
+    D = 12
+    pairs = [(0, 1), (2, 9), (5, 11), (10, 11)]
+    got = eng.pair_counts(t, bins, pairs)
+    want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, bins, pairs)
+    for p, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p
+
+
+def test_one_bin_above_1d_maximum_is_rejected(eng):
+    t = _synth_case(6, 100, 0, seed=8)
+    with pytest.raises(pg.PGError) as e:
+        eng.entropy(t, (16385, 50, 50, 50, 50, 50), "hist")
+    assert e.value.code == pg.PG_ERR_UNSUPPORTED
