@@ -14,6 +14,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <thread>
 #include <vector>
@@ -464,17 +465,63 @@ PG_API int pg_write_mie_text(const char *path, int n_dih, const pg_par_body *b) 
         const char *nm[6] = {"bond-bond ", "bond-angle ", "bond-dihedral ", "angle-angle ", "angle-dihedral ", "dihedral-dihedral "};
         const int n1[6] = {nb, nb, nb, na, na, nd}, n2[6] = {nb, na, nd, na, nd, nd};
         const double *blk[6] = {b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
+        // The block totals are summed in the reference's line order (one
+        // thread); the lines themselves are formatted by all host threads in
+        // row tasks of ~64k lines and written in order, a bounded batch at a time.
+        struct Task {
+            int q, i0, i1;
+        };
+        std::vector<Task> tasks;
         for (int q = 0; q < 6; q++) {
             const bool same = q == 0 || q == 3 || q == 5;
             int64_t counter = (int64_t)n1[q] * (n1[q] - 1) / 2 - 1;
-            for (int i = 0; i < (same ? n1[q] - 1 : n1[q]); i++)
+            const int rows = same ? n1[q] - 1 : n1[q];
+            int64_t acc = 0;
+            int i0 = 0;
+            for (int i = 0; i < rows; i++) {
                 for (int j = same ? i + 1 : 0; j < n2[q]; j++) {
                     const double mu = mutual(q, i, j, n_dih, b);
                     const double s2 = same ? blk[q][counter--] : blk[q][(int64_t)i * n2[q] + j];
-                    o.s(nm[q]).i(i + 1).s("  ").i(j + 1).s("   ").d(s2).s("   ").d(mu).s("\n");
                     e[q] += s2;
                     m[q] += mu;
                 }
+                acc += same ? n2[q] - i - 1 : n2[q];
+                if (acc >= 65536 || i == rows - 1) {
+                    tasks.push_back({q, i0, i + 1});
+                    i0 = i + 1;
+                    acc = 0;
+                }
+            }
+        }
+        auto format_rows = [&](const Task &t, std::string &out) {
+            const int q = t.q;
+            const bool same = q == 0 || q == 3 || q == 5;
+            const int64_t n = n1[q];
+            // reverse-order index of the first line of row i0
+            int64_t counter = n * (n - 1) / 2 - 1 - ((int64_t)t.i0 * (n - 1) - (int64_t)t.i0 * (t.i0 - 1) / 2);
+            char line[160];
+            for (int i = t.i0; i < t.i1; i++)
+                for (int j = same ? i + 1 : 0; j < n2[q]; j++) {
+                    const double mu = mutual(q, i, j, n_dih, b);
+                    const double s2 = same ? blk[q][counter--] : blk[q][(int64_t)i * n2[q] + j];
+                    const int k = snprintf(line, sizeof line, "%s%d  %d   %.12g   %.12g\n", nm[q], i + 1, j + 1, s2, mu);
+                    out.append(line, (size_t)k);
+                }
+        };
+        const int nthr = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        for (size_t t0 = 0; t0 < tasks.size(); t0 += (size_t)nthr * 4) {
+            const size_t t1 = std::min(tasks.size(), t0 + (size_t)nthr * 4);
+            std::vector<std::string> bufs(t1 - t0);
+            std::vector<std::thread> pool;
+            for (int w = 0; w < nthr; w++)
+                pool.emplace_back([&, w] {
+                    for (size_t k = t0 + w; k < t1; k += (size_t)nthr) format_rows(tasks[k], bufs[k - t0]);
+                });
+            for (auto &th : pool) th.join();
+            for (const std::string &sbuf : bufs) {
+                o.flush();
+                fwrite(sbuf.data(), 1, sbuf.size(), f);
+            }
         }
         o.s("TOTAL 1D BONDS ENTROPY = ").d(tB).s("\n");
         o.s("TOTAL 1D ANGLES ENTROPY = ").d(tA).s("\n");

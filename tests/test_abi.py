@@ -159,3 +159,42 @@ def test_engine_without_gpu_fails_loudly():
     with pytest.raises(pg.PGError) as e:
         pg.Engine(0)
     assert e.value.code in (pg.PG_ERR_CUDA, pg.PG_ERR_ARG)
+
+
+def test_mie_text_many_rows_matches_python_formatting(tmp_path):
+    """The MIE writer formats its lines on all host threads in row tasks; on a
+    body large enough for many tasks every line equals a single-threaded
+    %.12g rendering in the reference's order, and the totals match."""
+    import numpy as np
+    import oracle
+    n = 150
+    rng = np.random.default_rng(4)
+    sizes = pg.block_sizes(n)
+    blocks = {k: rng.normal(-3.0, 1.0, v) for k, v in sizes.items()}
+    body = pg.ParBody(n, blocks)
+    out = tmp_path / "mie.txt"
+    pg.write_mie_text(out, body)
+    lines = out.read_text().splitlines()
+    nb, na, nd = n + 2, n + 1, n
+    want = [f"bond {k + 1}   {blocks['s1_b'][k]:.12g}" for k in range(nb)]
+    want += [f"angle {k + 1}   {blocks['s1_a'][k]:.12g}" for k in range(na)]
+    want += [f"dihedral {k + 1}   {blocks['s1_d'][k]:.12g}" for k in range(nd)]
+    specs = [("bond-bond ", "bb", "s1_b", "s1_b", nb, nb, True), ("bond-angle ", "ba", "s1_b", "s1_a", nb, na, False),
+             ("bond-dihedral ", "bd", "s1_b", "s1_d", nb, nd, False), ("angle-angle ", "aa", "s1_a", "s1_a", na, na, True),
+             ("angle-dihedral ", "ad", "s1_a", "s1_d", na, nd, False),
+             ("dihedral-dihedral ", "dd", "s1_d", "s1_d", nd, nd, True)]
+    for name, key, a1, a2, n1, n2, same in specs:
+        arr = blocks[key]
+        if same:
+            i, j = np.triu_indices(n1, 1)
+            s2 = arr[::-1]
+        else:
+            i, j = np.divmod(np.arange(n1 * n2), n2)
+            s2 = arr
+        mu = blocks[a1][i] + blocks[a2][j] - s2
+        want += [f"{name}{a + 1}  {c + 1}   {x:.12g}   {y:.12g}" for a, c, x, y in zip(i, j, s2, mu)]
+    assert len(lines) == len(want) + 16
+    assert lines[:len(want)] == want
+    tot = oracle.mie_totals(n, blocks)
+    got_tot = np.array([float(ln.split(" = ")[1]) for ln in lines[len(want):]])
+    assert np.array_equal(np.array([float(oracle.fmt12(x)) for x in tot]), got_tot)
