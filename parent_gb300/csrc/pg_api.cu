@@ -1116,9 +1116,38 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         tiles.insert(tiles.end(), t.begin(), t.end());
         tsys.insert(tsys.end(), t.size(), s);
     }
+    // preprocessing of all systems in one launch per input precision: CTA
+    // k handles DOF map[k].y of system map[k].x
+    std::vector<PrepDesc> pd((size_t)n_sys);
+    std::vector<int2> pmap[2];
+    for (int s = 0; s < n_sys; s++) {
+        const BatchLayout &L = sys[s];
+        const pg_bat_view &v = trajs[s];
+        const size_t es = elem_size(v.double_prec);
+        PrepDesc &p = pd[s];
+        p.geo = L.g;
+        if (L.own_cols) {
+            const char *c = arena + L.cols;
+            p.cols[0] = c;
+            p.cols[1] = c + (size_t)L.g.nb * L.g.F * es;
+            p.cols[2] = L.g.nd ? c + (size_t)(L.g.nb + L.g.na) * L.g.F * es : p.cols[1];
+        } else {
+            p.cols[0] = v.bonds;
+            p.cols[1] = v.angles;
+            p.cols[2] = v.dihedrals ? v.dihedrals : v.angles;
+        }
+        p.ld = L.ld;
+        p.prec = L.prec;
+        p.dof = dofs_at(L);
+        p.bins = (uint8_t *)(arena + L.bins);
+        for (int g = 0; g < L.g.D; g++) pmap[L.prec].push_back(make_int2(s, g));
+    }
     const size_t mo_sd = 0, mo_md = al256(sizeof(SysDesc) * n_sys), mo_t = mo_md + al256(sizeof(MistDesc) * n_sys),
                  mo_ts = mo_t + al256(sizeof(PairTile) * std::max<size_t>(tiles.size(), 1)),
-                 mo_end = mo_ts + al256(sizeof(int) * std::max<size_t>(tsys.size(), 1));
+                 mo_pd = mo_ts + al256(sizeof(int) * std::max<size_t>(tsys.size(), 1)),
+                 mo_m0 = mo_pd + al256(sizeof(PrepDesc) * n_sys),
+                 mo_m1 = mo_m0 + al256(sizeof(int2) * std::max<size_t>(pmap[0].size(), 1)),
+                 mo_end = mo_m1 + al256(sizeof(int2) * std::max<size_t>(pmap[1].size(), 1));
     CK(ctx->batchmeta.ensure(mo_end));
     char *meta = (char *)ctx->batchmeta.p;
 
@@ -1150,6 +1179,11 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
             CK(cudaMemcpyAsync(meta + mo_t, tiles.data(), sizeof(PairTile) * tiles.size(), cudaMemcpyHostToDevice, st));
             CK(cudaMemcpyAsync(meta + mo_ts, tsys.data(), sizeof(int) * tsys.size(), cudaMemcpyHostToDevice, st));
         }
+        CK(cudaMemcpyAsync(meta + mo_pd, pd.data(), sizeof(PrepDesc) * n_sys, cudaMemcpyHostToDevice, st));
+        for (int q = 0; q < 2; q++)
+            if (!pmap[q].empty())
+                CK(cudaMemcpyAsync(meta + (q ? mo_m1 : mo_m0), pmap[q].data(), sizeof(int2) * pmap[q].size(),
+                                   cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));  // host vectors go out of scope
     }
     // host columns -> arena (outside the graph: their source is the caller's)
@@ -1176,25 +1210,13 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         cudaGraph_t graph = nullptr;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st);
+        for (int q = 0; q < 2 && e == cudaSuccess; q++)
+            e = launch_prep_batch(sys[0].g, (const PrepDesc *)(meta + mo_pd), (const int2 *)(meta + (q ? mo_m1 : mo_m0)),
+                                  (int)pmap[q].size(), q, (int *)ctx->errw.p, st);
         for (int s = 0; s < n_sys && e == cudaSuccess; s++) {
             const BatchLayout &L = sys[s];
-            const pg_bat_view &v = trajs[s];
-            const size_t es = elem_size(v.double_prec);
-            const void *cols[3];
-            if (L.own_cols) {
-                const char *c = arena + L.cols;
-                cols[0] = c;
-                cols[1] = c + (size_t)L.g.nb * L.g.F * es;
-                cols[2] = L.g.nd ? c + (size_t)(L.g.nb + L.g.na) * L.g.F * es : cols[1];
-            } else {
-                cols[0] = v.bonds;
-                cols[1] = v.angles;
-                cols[2] = v.dihedrals ? v.dihedrals : v.angles;
-            }
-            const DofArrays d = dofs_at(L);
-            e = launch_prep(L.g, cols, L.ld, L.prec, d, (uint8_t *)(arena + L.bins), (int *)ctx->errw.p, st);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(arena + L.par, d.s1, (size_t)L.g.D * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            e = cudaMemcpyAsync(arena + L.par, dofs_at(L).s1, (size_t)L.g.D * sizeof(double), cudaMemcpyDeviceToDevice,
+                                st);
         }
         if (e == cudaSuccess)
             e = h32 ? launch_pairs_hist32_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
@@ -1217,7 +1239,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         ctx->graph_key = key;
     }
     CK(cudaGraphLaunch(ctx->graph, st));
-    ctx->launches += n_sys + 2;  // one prep kernel per system, then the pair and MIST kernels
+    ctx->launches += (pmap[0].empty() ? 0 : 1) + (pmap[1].empty() ? 0 : 1) + 2;  // preps, pairs, MIST
     CK(cudaEventRecord(ctx->ev[2], st));
     int rc = check_err_words(ctx);
     float ms[2];

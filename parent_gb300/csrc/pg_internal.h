@@ -90,6 +90,20 @@ cudaError_t launch_nlogn_fix_table(unsigned long long *nfix, int nmax, double fi
 cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld, int double_prec,
                         DofArrays dof, uint8_t *bins, int *err, cudaStream_t st, int g_first = 0,
                         int g_count = -1);
+// One system's preprocessing inputs and outputs, for batched launches.
+struct PrepDesc {
+    SysGeom geo;
+    const void *cols[3];
+    int64_t ld;
+    int prec;
+    DofArrays dof;
+    uint8_t *bins;
+};
+// Preprocessing of many systems in one launch: CTA k handles DOF map[k].y of
+// system map[k].x; all systems have the input precision double_prec and the
+// bin counts of bins_of.
+cudaError_t launch_prep_batch(const SysGeom &bins_of, const PrepDesc *sys, const int2 *map, int n_cta,
+                              int double_prec, int *err, cudaStream_t st);
 
 // Shared-memory histogram pair kernel with fused entropy/MI epilogue.
 // If counts != nullptr the raw 2D histograms of each tile's first pair slots

@@ -74,15 +74,12 @@ __device__ __forceinline__ F2 split2(double v) {
 // region gives that region's extreme shifted value.
 constexpr int kRegions = 3;  // x in [0, 2 pi + 5e-9) and modFit in (0, 2 pi] give q in {0, 1, 2}
 
+// One CTA's work on DOF g of one system.
 template <bool F32>
-__global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb,
-                                                        const void *ca, const void *cd,
-                                                        int64_t ld, int prec, DofArrays dof,
-                                                        uint8_t *bins, int *err,
-                                                        double modfit_bs, double pi, int g_first,
-                                                        int h1_copies) {
+__device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, const void *ca, const void *cd,
+                                          int64_t ld, int prec, const DofArrays &dof, uint8_t *bins, int *err,
+                                          double modfit_bs, double pi, int g, int h1_copies) {
     extern __shared__ unsigned int sh[];
-    const int g = g_first + blockIdx.x;
     const int type = dof_type(g, geo.nb, geo.na);
     const int local = g - (type == TB ? 0 : (type == TA ? geo.nb : geo.nb + geo.na));
     const void *col = type == TB ? cb : (type == TA ? ca : cd);
@@ -393,6 +390,25 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
     }
 }
 
+template <bool F32>
+__global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb, const void *ca, const void *cd,
+                                                        int64_t ld, int prec, DofArrays dof, uint8_t *bins, int *err,
+                                                        double modfit_bs, double pi, int g_first, int h1_copies) {
+    prep_body<F32>(geo, cb, ca, cd, ld, prec, dof, bins, err, modfit_bs, pi, g_first + blockIdx.x, h1_copies);
+}
+
+// Many systems in one launch: CTA k preprocesses DOF map[k].y of system
+// map[k].x (systems of one input precision per launch).
+template <bool F32>
+__global__ void __launch_bounds__(kThreads) prep_batch_kernel(const PrepDesc *__restrict__ sys,
+                                                              const int2 *__restrict__ map, int *err,
+                                                              double modfit_bs, double pi, int h1_copies) {
+    const int2 m = map[blockIdx.x];
+    const PrepDesc &d = sys[m.x];
+    prep_body<F32>(d.geo, d.cols[0], d.cols[1], d.cols[2], d.ld, d.prec, d.dof, d.bins, err, modfit_bs, pi, m.y,
+                   h1_copies);
+}
+
 __global__ void nlogn_kernel(double *t, int nmax) {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
         t[n] = n > 1 ? (double)n * log((double)n) : 0.0;
@@ -453,6 +469,21 @@ cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld,
     const int c1 = prep_h1_copies(g, &m1, &m2);
     kern<<<g_count, kThreads, smem, st>>>(g, cols[0], cols[1], cols[2], ld, double_prec, dof, bins, err, modfit_bs,
                                           pi, g_first, c1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_batch(const SysGeom &bins_of, const PrepDesc *sys, const int2 *map, int n_cta,
+                              int double_prec, int *err, cudaStream_t st) {
+    if (n_cta <= 0) return cudaSuccess;
+    const double pi = acos(-1.0);  // PARENT.cpp:112
+    const double modfit_bs = (2 * pi + 0.000000005) / kModfitBins;  // PARENT.cpp:569
+    const size_t smem = prep_smem_bytes(bins_of);
+    int m1 = 0, m2 = 0;
+    const int c1 = prep_h1_copies(bins_of, &m1, &m2);
+    auto kern = double_prec ? prep_batch_kernel<false> : prep_batch_kernel<true>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<n_cta, kThreads, smem, st>>>(sys, map, err, modfit_bs, pi, c1);
     return cudaGetLastError();
 }
 
