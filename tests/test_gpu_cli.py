@@ -62,3 +62,49 @@ def test_parent_cli_form_override(tmp_path):
     for k in want:
         if want[k].size:
             assert np.max(np.abs(got[k] - want[k])) <= 1e-9, k
+
+
+def test_parent_cli_checkpoint_resume(tmp_path):
+    """PG_SHARDS=4 with an interruption after two shards (exit code 3, a
+    checkpoint left behind), then a rerun that resumes: the .par is
+    byte-identical to a one-pass run and the checkpoint is removed."""
+    import os
+    bat = GOLDEN / "synth_small.bat"
+    whole = tmp_path / "whole.par"
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(whole)] + ["50"] * 6,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "sharded.par"
+    ckpt = tmp_path / "sharded.par.ckpt"
+    env = dict(os.environ, PG_SHARDS="4", PG_STOP_AFTER_SHARDS="2")
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(out)] + ["50"] * 6,
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 3, r.stdout + r.stderr
+    assert ckpt.exists() and not out.exists()
+    env = dict(os.environ, PG_SHARDS="4")
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(out)] + ["50"] * 6,
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "Resuming" in r.stdout and "2 of 4" in r.stdout
+    assert not ckpt.exists()
+    assert out.read_bytes() == whole.read_bytes()
+
+
+def test_parent_cli_ignores_foreign_checkpoint(tmp_path):
+    """A checkpoint written for other bin counts is not resumed from."""
+    import os
+    bat = GOLDEN / "synth_small.bat"
+    out = tmp_path / "o.par"
+    env = dict(os.environ, PG_SHARDS="3", PG_STOP_AFTER_SHARDS="1")
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(out)] + ["40"] * 6,
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 3
+    env = dict(os.environ, PG_SHARDS="3")
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(out)] + ["50"] * 6,
+                       capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    assert "Resuming" not in r.stdout
+    whole = tmp_path / "w.par"
+    r = subprocess.run([str(BIN / "PARENT_gb300"), str(bat), str(whole)] + ["50"] * 6,
+                       capture_output=True, text=True, timeout=300)
+    assert out.read_bytes() == whole.read_bytes()
