@@ -23,10 +23,6 @@ constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kModfitBins = 100;  // PARENT.cpp:51
 
-__device__ __forceinline__ double load_val(const void *col, int prec, int64_t f) {
-    return prec ? __ldg((const double *)col + f) : (double)__ldg((const float *)col + f);
-}
-
 // q = int((x + modFit) / (2 pi)) and x + modFit - 2 pi q, PARENT.cpp:611,
 // evaluated as the reference's left-to-right expression without contraction.
 __device__ __forceinline__ int shift_quot(double t, double twopi) { return __double2int_rz(__ddiv_rn(t, twopi)); }
@@ -74,8 +70,27 @@ __device__ __forceinline__ F2 split2(double v) {
 // region gives that region's extreme shifted value.
 constexpr int kRegions = 3;  // x in [0, 2 pi + 5e-9) and modFit in (0, 2 pi] give q in {0, 1, 2}
 
-// One CTA's work on DOF g of one system.
-template <bool F32>
+// Order-preserving 64-bit image of a double for exact extrema on the
+// integer pipe (NaN mapped below everything for maxima, above for minima, so
+// it never wins either, as with the reference's strict comparisons).
+__device__ __forceinline__ unsigned long long okey_raw(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if (b == 0x8000000000000000ull) b = 0ull;  // -0 == +0
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ double okey_double(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// One CTA's work on DOF g of one system; T is the input element type (float
+// or double). Every bin decision is screened in FP32 (see above) with an
+// exact FP64 fallback; FP64 inputs enter the screen rounded to FP32, an
+// error the bounds below include.
+template <typename T>
 __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, const void *ca, const void *cd,
                                           int64_t ld, int prec, const DofArrays &dof, uint8_t *bins, int *err,
                                           double modfit_bs, double pi, int g, int h1_copies) {
@@ -85,7 +100,11 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const void *col = type == TB ? cb : (type == TA ? ca : cd);
     col = prec ? (const void *)((const double *)col + (int64_t)local * ld)
                : (const void *)((const float *)col + (int64_t)local * ld);
-    const float *colf = (const float *)col;
+    const T *colT = (const T *)col;
+    constexpr bool kDbl = sizeof(T) == 8;
+    // relative error bound factor of an FP32 quotient: 3 roundings (2^-23)
+    // for FP32 input, 4 for FP64 input rounded to FP32; both under 1/4 of it
+    constexpr float kQRel = kDbl ? 0x1p-20f : 0x1p-21f;
     const int F = geo.F;
     const int B1 = geo.bins[type], B2 = geo.bins[3 + type];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -98,25 +117,21 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const int w1 = h1_copies > 1 ? warp : 0;
     __shared__ double s_shift, s_mn, s_mx;
     __shared__ double red_mn[kWarps], red_mx[kWarps];
-    __shared__ float red_rmax[kWarps][kRegions], red_rmin[kWarps][kRegions];
 
     double modfit = 0.0;
     if (type == TD) {
         for (int k = tid; k < kWarps * kModfitBins; k += kThreads) hmod[k] = 0;
         __syncthreads();
         int bad = 0;
-        // x / modfit_bs: relative error of x32 * fl32(1/bs) <= 2^-23
+        // x / modfit_bs: relative error of x32 * fl32(1/bs) <= 2^-23 (2^-22.4
+        // with the FP32 rounding of an FP64 input)
         const float rm = __double2float_rn(__drcp_rn(modfit_bs));
         for (int f = tid; f < F; f += kThreads) {
-            int idx = -1;
-            if (F32) {
-                const float x = __ldg(colf + f);
-                const float q = __fmul_rn(x, rm);
-                idx = screened_floor(q, __fmul_ru(q, 0x1p-21f));
-                if (idx < 0) idx = __double2int_rz(__ddiv_rn((double)x, modfit_bs));
-            } else {
-                idx = __double2int_rz(__ddiv_rn(load_val(col, prec, f), modfit_bs));
-            }
+            const T xv = __ldg(colT + f);
+            const float x = (float)xv;
+            const float q = __fmul_rn(x, rm);
+            int idx = screened_floor(q, __fmul_ru(q, kQRel));
+            if (idx < 0) idx = __double2int_rz(__ddiv_rn((double)xv, modfit_bs));
             if (idx < 0 || idx >= kModfitBins) { bad++; idx = idx < 0 ? 0 : kModfitBins - 1; }
             atomicAdd(&hmod[warp * kModfitBins + idx], 1u);
         }
@@ -165,52 +180,62 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const F2 mf2 = split2(modfit), tp2 = split2(twopi);
     const float r2pi = __double2float_rn(__drcp_rn(twopi));
     constexpr float kShiftEps = 4e-6f;
-    // exact quotient q of the shift for an FP32 value (screened, else FP64)
-    auto shift_q = [&](float x, float &t32) -> int {
+    // exact quotient q of the shift of value xd (x = its FP32 rounding):
+    // screened, else FP64
+    auto shift_q = [&](float x, double xd, float &t32) -> int {
         t32 = __fadd_rn(__fadd_rn(x, mf2.hi), mf2.lo);
         int q = screened_floor(__fmul_rn(t32, r2pi), kShiftEps);
-        if (q < 0) q = shift_quot(__dadd_rn((double)x, modfit), twopi);
+        if (q < 0) q = shift_quot(__dadd_rn(xd, modfit), twopi);
         return q;
     };
 
-    // ---- extrema (PARENT.cpp:512-521, 539-548, 614-623)
+    // ---- extrema (PARENT.cpp:512-521, 539-548, 614-623): the largest and
+    // smallest input value of each shift-quotient region (exact: FP32 values
+    // compare exactly as floats, FP64 values through their integer images),
+    // then the shifted FP64 value of each candidate
     double lmax = -1.0e100, lmin = 1.0e100;
-    if (F32) {
-        float rmax[kRegions], rmin[kRegions];
-        for (int r = 0; r < kRegions; r++) { rmax[r] = -INFINITY; rmin[r] = INFINITY; }
+    {
+        unsigned long long kmax[kRegions], kmin[kRegions];
+        for (int r = 0; r < kRegions; r++) { kmax[r] = 0ull; kmin[r] = ~0ull; }
         for (int f = tid; f < F; f += kThreads) {
-            const float x = __ldg(colf + f);
+            const T xv = __ldg(colT + f);
+            const double xd = (double)xv;
             int r = 0;
             if (type == TD) {
                 float t32;
-                r = shift_q(x, t32);
+                r = shift_q((float)xv, xd, t32);
                 r = r < 0 ? 0 : (r >= kRegions ? kRegions - 1 : r);  // out of range: flagged above
             }
+            const bool nan = is_nan_bits(xd);
+            const unsigned long long k = okey_raw(xd);
 #pragma unroll
-            for (int k = 0; k < kRegions; k++) {
-                if (k == r) {
-                    rmax[k] = fmaxf(rmax[k], x);
-                    rmin[k] = fminf(rmin[k], x);
+            for (int q = 0; q < kRegions; q++) {
+                if (q == r && !nan) {
+                    kmax[q] = k > kmax[q] ? k : kmax[q];
+                    kmin[q] = k < kmin[q] ? k : kmin[q];
                 }
             }
         }
-        for (int k = 0; k < kRegions; k++) {
+        __shared__ unsigned long long red_kmax[kWarps][kRegions], red_kmin[kWarps][kRegions];
+        for (int q = 0; q < kRegions; q++) {
             for (int o = 16; o > 0; o >>= 1) {
-                rmax[k] = fmaxf(rmax[k], __shfl_xor_sync(0xffffffffu, rmax[k], o));
-                rmin[k] = fminf(rmin[k], __shfl_xor_sync(0xffffffffu, rmin[k], o));
+                const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmax[q], o);
+                const unsigned long long b = __shfl_xor_sync(0xffffffffu, kmin[q], o);
+                kmax[q] = a > kmax[q] ? a : kmax[q];
+                kmin[q] = b < kmin[q] ? b : kmin[q];
             }
-            if (lane == 0) { red_rmax[warp][k] = rmax[k]; red_rmin[warp][k] = rmin[k]; }
+            if (lane == 0) { red_kmax[warp][q] = kmax[q]; red_kmin[warp][q] = kmin[q]; }
         }
         __syncthreads();
         if (tid == 0) {
-            for (int k = 0; k < kRegions; k++) {
-                float a = -INFINITY, b = INFINITY;
+            for (int q = 0; q < kRegions; q++) {
+                unsigned long long a = 0ull, b = ~0ull;
                 for (int w = 0; w < kWarps; w++) {
-                    a = fmaxf(a, red_rmax[w][k]);
-                    b = fminf(b, red_rmin[w][k]);
+                    a = red_kmax[w][q] > a ? red_kmax[w][q] : a;
+                    b = red_kmin[w][q] < b ? red_kmin[w][q] : b;
                 }
                 if (a < b) continue;  // empty region
-                double va = (double)a, vb = (double)b;
+                double va = okey_double(a), vb = okey_double(b);
                 if (type == TD) {
                     va = shifted(va, modfit, twopi);
                     vb = shifted(vb, modfit, twopi);
@@ -221,25 +246,11 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             red_mx[0] = lmax;
             red_mn[0] = lmin;
         }
-    } else {
-        for (int f = tid; f < F; f += kThreads) {
-            double x = load_val(col, prec, f);
-            if (type == TD) x = shifted(x, modfit, twopi);
-            if (x > lmax) lmax = x;
-            if (x < lmin) lmin = x;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const double a = __shfl_xor_sync(0xffffffffu, lmax, o);
-            const double b = __shfl_xor_sync(0xffffffffu, lmin, o);
-            if (a > lmax) lmax = a;
-            if (b < lmin) lmin = b;
-        }
-        if (lane == 0) { red_mx[warp] = lmax; red_mn[warp] = lmin; }
     }
     __syncthreads();
     if (tid == 0) {
         double tmpMax = -1.0e100, tmpMin = 1.0e100;
-        for (int w = 0; w < (F32 ? 1 : kWarps); w++) {
+        for (int w = 0; w < 1; w++) {
             if (red_mx[w] > tmpMax) tmpMax = red_mx[w];
             if (red_mn[w] < tmpMin) tmpMin = red_mn[w];
         }
@@ -266,11 +277,12 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
     uint8_t *brow = bins + (int64_t)g * geo.ldb;
     int bad = 0;
-    if (F32) {
+    {
         // d = fl64(x' - mn) (x' the shifted value for dihedrals) is formed in
         // FP32 from split constants, |d32 - d| <= 2^-20 E with
         // E = |mn| + |mx| (+ 2|modFit| + 8 pi for dihedrals), a bound >= 4x
-        // the accumulated rounding; q_k = d32 * fl32(1 / bs_k) then has
+        // the accumulated rounding (including an FP64 input's rounding to
+        // FP32, <= 2^-24 E); q_k = d32 * fl32(1 / bs_k) then has
         // |q_k - q*| <= 2^-20 E / bs_k + 2^-22 q_k.
         const F2 mn2 = split2(mn);
         const float r1 = __double2float_rn(__drcp_rn(bs1)), r2 = __double2float_rn(__drcp_rn(bs2));
@@ -278,12 +290,13 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
         if (type == TD) E = E + 2.0 * fabs(modfit) + 4.0 * twopi;
         const float e1 = __double2float_ru(E * 0x1p-20 / bs1), e2 = __double2float_ru(E * 0x1p-20 / bs2);
         for (int f = tid; f < F; f += kThreads) {
-            const float x = __ldg(colf + f);
+            const T xin = __ldg(colT + f);
+            const float x = (float)xin;
             float d32;
             int q = 0;
             if (type == TD) {
                 float t32;
-                q = shift_q(x, t32);
+                q = shift_q(x, (double)xin, t32);
                 const float qf = (float)q;
                 d32 = __fsub_rn(__fsub_rn(__fsub_rn(__fsub_rn(t32, __fmul_rn(qf, tp2.hi)), __fmul_rn(qf, tp2.lo)),
                                           mn2.hi),
@@ -292,26 +305,14 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
                 d32 = __fsub_rn(__fsub_rn(x, mn2.hi), mn2.lo);
             }
             const float q1 = __fmul_rn(d32, r1), q2 = __fmul_rn(d32, r2);
-            int i1 = screened_floor(q1, __fadd_ru(e1, __fmul_ru(fabsf(q1), 0x1p-21f)));
-            int i2 = screened_floor(q2, __fadd_ru(e2, __fmul_ru(fabsf(q2), 0x1p-21f)));
+            int i1 = screened_floor(q1, __fadd_ru(e1, __fmul_ru(fabsf(q1), kQRel)));
+            int i2 = screened_floor(q2, __fadd_ru(e2, __fmul_ru(fabsf(q2), kQRel)));
             if (i1 < 0 || i2 < 0) {
-                double xv = (double)x;
+                double xv = (double)xin;
                 if (type == TD) xv = shift_apply(__dadd_rn(xv, modfit), q, twopi);
                 if (i1 < 0) i1 = bin_index(xv, mn, bs1);
                 if (i2 < 0) i2 = bin_index(xv, mn, bs2);
             }
-            if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
-            if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
-            atomicAdd(&h1[w1 * B1 + i1], 1u);
-            atomicAdd(&h2[warp * B2 + i2], 1u);
-            brow[f] = (uint8_t)i2;
-        }
-    } else {
-        for (int f = tid; f < F; f += kThreads) {
-            double x = load_val(col, prec, f);
-            if (type == TD) x = shifted(x, modfit, twopi);
-            int i1 = bin_index(x, mn, bs1);
-            int i2 = bin_index(x, mn, bs2);
             if (i1 < 0 || i1 >= B1) { bad++; i1 = i1 < 0 ? 0 : B1 - 1; }
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
             atomicAdd(&h1[w1 * B1 + i1], 1u);
@@ -390,22 +391,22 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     }
 }
 
-template <bool F32>
+template <typename T>
 __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb, const void *ca, const void *cd,
                                                         int64_t ld, int prec, DofArrays dof, uint8_t *bins, int *err,
                                                         double modfit_bs, double pi, int g_first, int h1_copies) {
-    prep_body<F32>(geo, cb, ca, cd, ld, prec, dof, bins, err, modfit_bs, pi, g_first + blockIdx.x, h1_copies);
+    prep_body<T>(geo, cb, ca, cd, ld, prec, dof, bins, err, modfit_bs, pi, g_first + blockIdx.x, h1_copies);
 }
 
 // Many systems in one launch: CTA k preprocesses DOF map[k].y of system
 // map[k].x (systems of one input precision per launch).
-template <bool F32>
+template <typename T>
 __global__ void __launch_bounds__(kThreads) prep_batch_kernel(const PrepDesc *__restrict__ sys,
                                                               const int2 *__restrict__ map, int *err,
                                                               double modfit_bs, double pi, int h1_copies) {
     const int2 m = map[blockIdx.x];
     const PrepDesc &d = sys[m.x];
-    prep_body<F32>(d.geo, d.cols[0], d.cols[1], d.cols[2], d.ld, d.prec, d.dof, d.bins, err, modfit_bs, pi, m.y,
+    prep_body<T>(d.geo, d.cols[0], d.cols[1], d.cols[2], d.ld, d.prec, d.dof, d.bins, err, modfit_bs, pi, m.y,
                    h1_copies);
 }
 
@@ -462,7 +463,7 @@ cudaError_t launch_prep(const SysGeom &g, const void *const cols[3], int64_t ld,
     const double pi = acos(-1.0);  // PARENT.cpp:112
     const double modfit_bs = (2 * pi + 0.000000005) / kModfitBins;  // PARENT.cpp:569
     const size_t smem = prep_smem_bytes(g);
-    auto kern = double_prec ? prep_kernel<false> : prep_kernel<true>;
+    auto kern = double_prec ? prep_kernel<double> : prep_kernel<float>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int m1 = 0, m2 = 0;
@@ -480,7 +481,7 @@ cudaError_t launch_prep_batch(const SysGeom &bins_of, const PrepDesc *sys, const
     const size_t smem = prep_smem_bytes(bins_of);
     int m1 = 0, m2 = 0;
     const int c1 = prep_h1_copies(bins_of, &m1, &m2);
-    auto kern = double_prec ? prep_batch_kernel<false> : prep_batch_kernel<true>;
+    auto kern = double_prec ? prep_batch_kernel<double> : prep_batch_kernel<float>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<n_cta, kThreads, smem, st>>>(sys, map, err, modfit_bs, pi, c1);

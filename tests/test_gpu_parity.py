@@ -347,6 +347,74 @@ def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
         assert np.array_equal(x, y), p
 
 
+def _boundary_column64(rng, lo, hi, Bs, F, pad=5e-9):
+    """FP64 column on [lo, hi] holding the doubles adjacent to every bin edge
+    mn + k*bs, closer to the edges than any FP32 value can be."""
+    mn, mx = lo - pad, hi + pad
+    vals = [lo, hi]
+    for B in Bs:
+        bs = (mx - mn) / B
+        for k in range(1, B):
+            e = mn + k * bs
+            vals += [np.nextafter(e, -np.inf), e, np.nextafter(e, np.inf)]
+    vals = np.array([v for v in vals if lo <= v <= hi], dtype=np.float64)
+    fill = rng.uniform(lo, hi, F - vals.size)
+    col = np.concatenate([vals, fill])
+    rng.shuffle(col)
+    return col
+
+
+def test_fp64_bin_edges_bit_exact(eng):
+    """FP64 inputs go through the same FP32 screen after rounding to FP32:
+    doubles within one ulp of every 1D and 2D edge get the reference's bins."""
+    rng = np.random.default_rng(77)
+    n_dih, F = 2, 25000
+    B1, B2 = 41, 50
+    bins = (B1, B1, B1, B2, B2, B2)
+    bonds = np.stack([_boundary_column64(rng, 1.01 + 0.02 * k, 1.09 + 0.01 * k, (B1, B2), F) for k in range(n_dih + 2)])
+    angles = np.stack([_boundary_column64(rng, 1.7 + 0.05 * k, 2.2, (B1, B2), F) for k in range(n_dih + 1)])
+    base = [rng.uniform(0.5, 5.0, F), rng.uniform(0.0, 2 * np.pi - 1e-3, F)]
+    dih = []
+    for col in base:
+        tb = np.zeros((3, F)) + 1.0
+        ta = np.zeros((2, F)) + 1.5
+        mn, mx, sh, _, bad = oracle.extrema(tb, ta, col[None, :])
+        assert bad == 0
+        twopi = 2 * np.pi
+        extra = []
+        for B in (B1, B2):
+            for k in range(1, B):
+                t = mn[-1] + k * (mx[-1] - mn[-1]) / B
+                x = t - sh[-1]
+                if x < 0:
+                    x += twopi
+                extra += [np.nextafter(x, -np.inf), x, np.nextafter(x, np.inf)]
+        e = twopi - sh[-1]
+        extra += [np.nextafter(e, -np.inf), e, np.nextafter(e, np.inf)]
+        extra = np.array(extra)
+        extra = extra[(extra >= col.min()) & (extra <= col.max())]
+        c = col.copy()
+        c[rng.choice(F, extra.size, replace=False)] = extra
+        dih.append(c)
+    dih = np.stack(dih)
+    traj = pg.Trajectory(np.ascontiguousarray(bonds), np.ascontiguousarray(angles), np.ascontiguousarray(dih))
+    D = 3 * n_dih + 3
+    pairs = [(i, j) for i in range(D) for j in range(i + 1, D)]
+    got = eng.pair_counts(traj, bins, pairs)
+    want = oracle.pair_counts(bonds, angles, dih, bins, pairs)
+    for p_, x, y in zip(pairs, got, want):
+        assert np.array_equal(x, y), p_
+    mn, mx, sh = eng.dof_stats(D)
+    omn, omx, osh, _, bad = oracle.extrema(bonds, angles, dih)
+    assert bad == 0
+    assert np.array_equal(mn.view(np.uint64), omn.view(np.uint64))
+    assert np.array_equal(mx.view(np.uint64), omx.view(np.uint64))
+    assert np.array_equal(sh.view(np.uint64), osh.view(np.uint64))
+    body = eng.entropy(traj, bins, "hist")
+    ref = oracle.parent(bonds, angles, dih, bins)
+    compare_bodies(n_dih, body, ref)
+
+
 def _boundary_column(rng, lo, hi, Bs, F, pad=5e-9):
     """FP32 column on [lo, hi] (both present) packed with the float values
     next to every bin edge mn + k*bs (mn = lo - pad, mx = hi + pad) of each
