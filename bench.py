@@ -182,10 +182,43 @@ def cpu_sample(args, wl):
     D = 3 * na - 6
     units = D * (D - 1) // 2 * F
     t0 = time.perf_counter()
-    oracle.parent(t.bonds, t.angles, t.dihedrals, (args.bins,) * 6)
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, (args.bins,) * 6)
     dt = time.perf_counter() - t0
     sample = f"{D} DOFs ({na} atoms) x {F} frames of the same generator, {units:.3e} updates, {dt:.2f} s"
+    cpu_sample.last = (t, ref)  # the checker's result on the sample, for parity_on_sample
     return units / dt, sample, threads, dt
+
+
+def _mutual_all(n: int, body: dict):
+    """Every pair's MI as get_mutual (util.cpp:47-81) forms it, in body order."""
+    import numpy as np
+    nb, na = n + 2, n + 1
+    s1 = {"b": body["s1_b"], "a": body["s1_a"], "d": body["s1_d"]}
+    out = []
+    for key, t1, t2, n1 in (("bb", "b", "b", nb), ("ba", "b", "a", nb), ("bd", "b", "d", nb),
+                            ("aa", "a", "a", na), ("ad", "a", "d", na), ("dd", "d", "d", n)):
+        blk = body[key]
+        if blk.size == 0:
+            continue
+        if t1 == t2:
+            i, j = np.triu_indices(n1, 1)
+            out.append(s1[t1][i] + s1[t2][j] - blk[::-1])
+        else:
+            out.append((s1[t1][:, None] + s1[t2][None, :]).ravel() - blk)
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+def parity_on_sample(eng, bins, form):
+    """The GPU path on the CPU baseline's sample against the checker's FP64
+    result there: the largest |dS| and |dMI| (nats) over every term."""
+    import numpy as np
+    t, ref = cpu_sample.last
+    body = eng.entropy(t, bins, form)
+    ds = max(float(np.max(np.abs(body.blocks[k] - ref[k]), initial=0.0)) for k in body.blocks)
+    dmi = float(np.max(np.abs(_mutual_all(t.n_dih, body.blocks) - _mutual_all(t.n_dih, ref)), initial=0.0))
+    return {"max_abs_dS_nats": ds, "max_abs_dMI_nats": dmi, "mi_tolerance_nats": 1e-5,
+            "terms": int(sum(v.size for v in ref.values())), "form": eng.last_form(),
+            "counts": "bit-exact (tests/test_gpu_parity.py)"}
 
 
 def run_reference(args):
@@ -354,11 +387,12 @@ def run_batch(args):
                 "frac": achieved / red_peak, "traffic": None,
                 "note": "whole captured graph (64 preps + one pair launch + one MIST launch) timed; one "
                         "shared-memory reduction per update; peak = live conflict-free red.shared rate"}
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, sample, threads, _ = cpu_sample(args, (800, 31_700, 0, 0.0, 0.0, 8))
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": sample + " (one system of the batch's largest atom count at its mean frame count)"}
+        parity = parity_on_sample(eng, bins, args.form)
     if rank == 0:
         Ds = [3 * a - 6 for a, _, _, _ in systems]
         Fs = [f for _, f, _, _ in systems]
@@ -374,7 +408,7 @@ def run_batch(args):
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (total_bytes / 1e9)},
             "sequential": {"ms_per_step": ms_seq, "value": units * world / (ms_seq / 1e3),
                            "speedup_of_batch": ms_seq / ms_batch},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
     eng.free(dbuf)
@@ -529,10 +563,11 @@ def run_gb300(args):
                      "frac": prep_bytes / prep_s / 1e9 / hbm,
                      "note": "algorithmic bytes D*F*(4|8 in + 1 bin out); peak of measured copy bandwidth"}
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, sample, threads, _ = cpu_sample(args, WORKLOADS[args.workload])
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+        parity = parity_on_sample(eng, bins, args.form)
 
     if rank == 0:
         line = {
@@ -547,7 +582,7 @@ def run_gb300(args):
             "kernel_ms": {"prep": statistics.mean(prep_ms), "pairs": statistics.mean(pair_ms),
                           "mist": statistics.mean(mist_ms)},
             "roofline": roofline, "roofline_prep": roofline_prep,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
     eng.free(dbuf)

@@ -244,6 +244,23 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     return PG_OK;
 }
 
+// Enqueues the copies of a device .par body (layout L) into the caller's
+// host blocks; every non-empty block needs a destination.
+static int body_to_host(pg_ctx *ctx, const double *par, const ParLayout &L, const pg_par_body *out, int sys) {
+    double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
+    const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
+    for (int k = 0; k < 9; k++) {
+        const int64_t n = off[k + 1] - off[k];
+        if (n <= 0) continue;
+        if (!dst[k]) {
+            if (sys >= 0) return fail(ctx, PG_ERR_ARG, "system %d: null output block %d", sys, k);
+            return fail(ctx, PG_ERR_ARG, "null output block %d", k);
+        }
+        CK(cudaMemcpyAsync(dst[k], par + off[k], (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return PG_OK;
+}
+
 static int check_err_words(pg_ctx *ctx) {
     int h[ERR_WORDS];
     CK(cudaMemcpyAsync(h, ctx->errw.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
@@ -447,15 +464,8 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
                        st));
     CK(cudaEventRecord(ctx->ev[1], st));
     if (out) {
-        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
-        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
-        for (int k = 0; k < 9; k++) {
-            const int64_t n = off[k + 1] - off[k];
-            if (n <= 0) continue;
-            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
-            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, st));
-        }
+        const int rcb = body_to_host(ctx, (const double *)ctx->par.p, L, out, -1);
+        if (rcb) return rcb;
     }
     CK(cudaEventRecord(ctx->ev[2], st));
     rc = check_err_words(ctx);
@@ -592,15 +602,8 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     ctx->last_form = chosen;
     CK(cudaEventRecord(ctx->ev[3], st));
     if (out) {
-        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
-        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
-        for (int k = 0; k < 9; k++) {
-            const int64_t n = off[k + 1] - off[k];
-            if (n <= 0) continue;
-            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
-            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, st));
-        }
+        const int rcb = body_to_host(ctx, (const double *)ctx->par.p, L, out, -1);
+        if (rcb) return rcb;
     }
     CK(cudaEventRecord(ctx->ev[4], st));
     rc = check_err_words(ctx);
@@ -698,15 +701,8 @@ PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins
         CK(cudaStreamSynchronize(st));  // the private tile buffer is released on return
     }
     if (out) {
-        double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
-        const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
-        for (int k = 0; k < 9; k++) {
-            const int64_t n = off[k + 1] - off[k];
-            if (n <= 0) continue;
-            if (!dst[k]) return fail(ctx, PG_ERR_ARG, "null output block %d", k);
-            CK(cudaMemcpyAsync(dst[k], (double *)ctx->par.p + off[k], (size_t)n * sizeof(double),
-                               cudaMemcpyDeviceToHost, st));
-        }
+        const int rcb = body_to_host(ctx, (const double *)ctx->par.p, L, out, -1);
+        if (rcb) return rcb;
     }
     rc = check_err_words(ctx);
     if (rc) return rc;
@@ -1258,16 +1254,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         const BatchLayout &L = sys[s];
         const ParLayout PL = par_layout(L.g.n_dih);
         if (outs) {
-            pg_par_body &o = outs[s];
-            double *dst[9] = {o.s1_b, o.s1_a, o.s1_d, o.bb, o.ba, o.bd, o.aa, o.ad, o.dd};
-            const int64_t po[10] = {PL.s1b, PL.s1a, PL.s1d, PL.bb, PL.ba, PL.bd, PL.aa, PL.ad, PL.dd, PL.total};
-            for (int k = 0; k < 9; k++) {
-                const int64_t n = po[k + 1] - po[k];
-                if (n <= 0) continue;
-                if (!dst[k]) return fail(ctx, PG_ERR_ARG, "system %d: null output block %d", s, k);
-                CK(cudaMemcpyAsync(dst[k], (double *)(arena + L.par) + po[k], (size_t)n * sizeof(double),
-                                   cudaMemcpyDeviceToHost, st));
-            }
+            const int rcb = body_to_host(ctx, (const double *)(arena + L.par), PL, &outs[s], s);
+            if (rcb) return rcb;
         }
         if ((edges && edges[s]) || totals) {
             const int D = L.g.D;
