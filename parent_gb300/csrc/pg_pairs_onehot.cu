@@ -9,9 +9,10 @@
 //
 // One CTA computes one 128 x 512 tile of C over all frames with
 // tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256, K=32, two accumulators
-// sharing the A tile): A and B are E4M3 one-hot tiles (1.0 = 0x38, 0.0 = 0x00)
+// sharing the A tile): A and B are E4M3 one-hot tiles (2.0 = 0x40, 0.0 = 0x00)
 // built in shared memory from the uint8 bin rows, the accumulators are FP32
-// in tensor memory (all 512 columns) and exact for counts below 2^24. Sixteen
+// in tensor memory (all 512 columns) holding 4 x the count, exact below 2^24
+// (frames below 2^22). Sixteen
 // warps expand 128-frame K-blocks into a 2-stage ring while one elected thread
 // issues the eight MMAs per block and commits them to the stage's mbarrier; a
 // stage is rebuilt only after its MMAs completed.
@@ -96,15 +97,15 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kNH >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
 
-// E4M3 one-hot of 4 bins against a bin replicated in t4: 0x38 (1.0) in every
-// byte where w equals t4, 0x00 elsewhere. x = w ^ t4 has a zero byte exactly
-// where they match; adding 0x7F to the low 7 bits of each byte sets bit 7 of
-// every byte that is nonzero without carrying into its neighbour, so the
-// complement of (sum | x | 0x7F7F7F7F) keeps bit 7 of the zero bytes only.
+// E4M3 one-hot of 4 bins against a bin replicated in t4: 0x40 (2.0) in every
+// byte where w equals t4, 0x00 elsewhere (bins below 128). x = w ^ t4 has a
+// zero byte exactly where they match and every byte below 128, so adding
+// 0x7F to each byte sets its bit 7 exactly when it is nonzero, without a
+// carry into the next byte; the complement's bit 7, shifted down by one, is
+// 2.0 in E4M3. Four integer operations per four frames.
 __device__ __forceinline__ uint32_t onehot4(uint32_t w, uint32_t t4) {
-    const uint32_t x = w ^ t4;
-    const uint32_t y = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
-    return (y >> 7) * 0x38u;
+    const uint32_t a = (w ^ t4) + 0x7F7F7F7Fu;
+    return (~a & 0x80808080u) >> 1;
 }
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
@@ -351,7 +352,7 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             if (cdof < 0) break;        // past the last row of C
             if (cdof <= rdof) continue;  // only pairs g1 < g2
             if (cdof != cur) flush(cdof);
-            const unsigned int n = (unsigned int)__float2uint_rn(__uint_as_float(v[q]));
+            const unsigned int n = (unsigned int)__float2uint_rn(__uint_as_float(v[q])) >> 2;  // 2.0 x 2.0 per frame
             if (n) {
                 snl += (unsigned long long)__ldg(nlogn_fix + n);
                 occ++;
@@ -446,8 +447,9 @@ static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles) {
 
 bool pairs_onehot_supported(const SysGeom &g) {
     for (int t = 0; t < 3; t++)
-        if (g.bins[3 + t] < 8 || g.bins[3 + t] > 255) return false;  // per-tile DOF tables sized for >= 8 bins
-    return g.F < (1 << 24);  // FP32 accumulators are exact below 2^24
+        if (g.bins[3 + t] < 8 || g.bins[3 + t] > 127) return false;  // per-tile DOF tables sized for >= 8 bins;
+                                                                     // bin bytes below 128 for the one-hot build
+    return g.F < (1 << 22);  // FP32 accumulators hold 4 x count, exact below 2^24
 }
 
 size_t pairs_onehot_scratch_bytes(const SysGeom &g) { return plan(g, nullptr).total; }
@@ -492,15 +494,15 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
 }
 
 // Form choice, from measured GB300 pair-kernel times at 2,994 DOFs x 100,000
-// frames: the histogram form takes 85.5 ms at any bin count up to 32 (32-slot
+// frames: the histogram form takes 85.6 ms at any bin count up to 32 (32-slot
 // layout, one conflict-free shared-memory reduction per update) and 117.6 ms
-// from 36 to 50 (16-slot layout); the one-hot form takes 45.9 / 58.5 / 71.3 /
-// 86.4 / 101.6 ms at 8 / 9 / 10 / 11 / 12 bins (B1*B2 FP8 MACs per update, so
-// its time grows as B^2). The one-hot form wins up to 10 bins.
+// from 36 to 50 (16-slot layout); the one-hot form takes 41.8 / 53.7 / 65.2 /
+// 79.1 / 92.9 ms at 8 / 9 / 10 / 11 / 12 bins (B1*B2 FP8 MACs per update, so
+// its time grows as B^2). The one-hot form wins up to 11 bins.
 int autotune_form(const SysGeom &g) {
     int bmax = 0;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (pairs_onehot_supported(g) && bmax <= 10 && g.F >= 4096) return PG_FORM_ONEHOT;
+    if (pairs_onehot_supported(g) && bmax <= 11 && g.F >= 4096) return PG_FORM_ONEHOT;
     return PG_FORM_HIST;
 }
 

@@ -194,10 +194,13 @@ def test_onehot_and_hist_agree_on_fixture(eng):
     assert np.max(np.abs(a - b)) <= S_TOL
 
 
-def test_onehot_rejects_tiny_bins(eng):
+@pytest.mark.parametrize("bins", [(50, 50, 50, 4, 50, 50), (50, 50, 50, 50, 128, 50)])
+def test_onehot_rejects_unsupported_bins(eng, bins):
+    """The one-hot form takes 2D bin counts 8..127 (per-tile DOF tables; bin
+    bytes below 128 for its one-hot build)."""
     t = _synth_case(10, 300, 1, seed=4)
     with pytest.raises(pg.PGError) as e:
-        eng.entropy(t, (50, 50, 50, 4, 50, 50), "onehot")
+        eng.entropy(t, bins, "onehot")
     assert e.value.code == pg.PG_ERR_UNSUPPORTED
 
 
