@@ -12,10 +12,12 @@
 // sharing the A tile): A and B are E4M3 one-hot tiles (2.0 = 0x40, 0.0 = 0x00)
 // built in shared memory from the uint8 bin rows, the accumulators are FP32
 // in tensor memory (all 512 columns) holding 4 x the count, exact below 2^24
-// (frames below 2^22). Sixteen
-// warps expand 128-frame K-blocks into a 2-stage ring while one elected thread
-// issues the eight MMAs per block and commits them to the stage's mbarrier; a
-// stage is rebuilt only after its MMAs completed.
+// (frames below 2^22). Warp-specialised: 15 builder warps load the tile's bin
+// rows two 128-frame K-blocks ahead (a 4-buffer ring) and expand each K-block
+// into a 2-stage ring of one-hot tiles, arriving on the stage's "full"
+// mbarrier; warp 15 waits on it, issues the block's eight MMAs and commits
+// them to the stage's "empty" mbarrier, which the builders wait on before
+// rebuilding the stage. No CTA-wide barrier inside the K loop.
 //
 // Epilogue: tcgen05.ld brings each row's counts to registers; every count n>0
 // of a pair (g1 < g2) adds round(2^s n ln n) (an int64 table) and 1 to the
@@ -30,12 +32,16 @@
 
 #include "../../include/parent_gb300.h"
 #include "pg_internal.h"
+#include "pg_sync.cuh"
 
 namespace pg {
 
 namespace {
 
-constexpr int kThreads = 512;          // 16 warps: builders; warp 0 lane 0 also issues MMAs
+constexpr int kThreads = 512;          // 16 warps: 15 load bin rows and build one-hot tiles, warp 15 issues MMAs
+constexpr int kBuilderWarps = 15;
+constexpr int kBuilders = kBuilderWarps * 32;
+constexpr int kLoaderWarp = 15;
 constexpr int kM = 128, kN = 512;      // tile of C: two 128 x 256 accumulators share one A tile
 constexpr int kNH = 256;               // N of one MMA
 constexpr int kKB = 128;               // frames per K-block (bytes per row per stage)
@@ -46,13 +52,16 @@ constexpr int kStageBytes = kAStage + kBStage;
 constexpr int kMaxRowDofs = 18, kMaxColDofs = 66;  // 2D bins >= 8
 constexpr int kBinSlots = kMaxRowDofs + kMaxColDofs;
 constexpr int kBinBufBytes = kBinSlots * kKB;      // one K-block of the tile's bin rows
+constexpr int kBinBufs = 4;                        // ring of K-block bin rows, loaded two blocks ahead
 // byte offsets inside the dynamic shared memory
-constexpr int kOffBar = kStages * kStageBytes;
-constexpr int kOffTmem = kOffBar + kStages * 8;
+constexpr int kOffBar = kStages * kStageBytes;     // full[kStages] | empty[kStages] | binfull[kBinBufs]
+constexpr int kNumBars = 2 * kStages + kBinBufs;
+constexpr int kOffTmem = kOffBar + kNumBars * 8;
 constexpr int kOffPsSnl = (kOffTmem + 16 + 15) / 16 * 16;
 constexpr int kOffPsOcc = kOffPsSnl + kMaxRowDofs * kMaxColDofs * 8;
 constexpr int kOffBins = (kOffPsOcc + kMaxRowDofs * kMaxColDofs * 4 + 127) / 128 * 128;
-constexpr int kSmemBytes = kOffBins + 2 * kBinBufBytes;
+constexpr int kSmemBytes = kOffBins + kBinBufs * kBinBufBytes;
+static_assert(kSmemBytes <= 227 * 1024, "one-hot kernel shared memory");
 constexpr long long kWaitCycles = 4000000000LL;
 // Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
 
@@ -72,6 +81,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     return ok != 0;
+}
+// arrive (release at CTA scope): the thread's earlier shared-memory writes
+// are visible to whoever completes the phase's wait
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
     const long long t0 = clock64();
@@ -144,12 +158,16 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
               int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *stages = smem;  // kStages x (A | B), 1024-B aligned
-    uint64_t *mma_done = (uint64_t *)(smem + kOffBar);
+    uint64_t *full = (uint64_t *)(smem + kOffBar);  // stage built (one arrival per builder warp)
+    uint64_t *empty = full + kStages;               // stage's MMAs done (tcgen05.commit)
+    uint64_t *binfull = empty + kStages;            // K-block bin rows stored (one arrival per builder warp)
     uint32_t *tmem_slot = (uint32_t *)(smem + kOffTmem);
     unsigned long long *ps_snl = (unsigned long long *)(smem + kOffPsSnl);  // [kMaxRowDofs][kMaxColDofs]
     unsigned int *ps_occ = (unsigned int *)(smem + kOffPsOcc);
     __shared__ int s_r0dof, s_c0dof;
     __shared__ int s_cdof[kN];  // DOF of each column of the tile (-1 past R)
+    __shared__ volatile int s_abort;
+    __shared__ int s_mma_issued;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const TcTile tile = tiles[blockIdx.x];
@@ -163,10 +181,16 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     }
     for (int c = tid; c < kN; c += kThreads) s_cdof[c] = c0 + c < R ? (int)(rowinfo[c0 + c] >> 8) : -1;
     if (tid == 0) {
-        for (int s = 0; s < kStages; s++) mbar_init(smem_u32(&mma_done[s]), 1);
+        for (int k = 0; k < kStages; k++) {
+            mbar_init(smem_u32(&full[k]), kBuilderWarps);
+            mbar_init(smem_u32(&empty[k]), 1);
+        }
+        for (int k = 0; k < kBinBufs; k++) mbar_init(smem_u32(&binfull[k]), kBuilderWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_r0dof = (int)(rowinfo[r0] >> 8);
         s_c0dof = (int)(rowinfo[c0 < R ? c0 : R - 1] >> 8);
+        s_abort = 0;
+        s_mma_issued = 0;
     }
     for (int i = tid; i < kMaxRowDofs * kMaxColDofs; i += kThreads) {
         ps_snl[i] = 0ull;
@@ -179,134 +203,160 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     const int rdof0 = s_r0dof, cdof0 = s_c0dof;
     const int rlast = (int)(rowinfo[min(r0 + kM, R) - 1] >> 8);
     const int clast = (int)(rowinfo[min(c0 + kN, R) - 1] >> 8);
-
-    // Shared double buffer of the tile's bin rows for one K-block,
-    // [2][kBinSlots][kKB]: slot k < kMaxRowDofs holds DOF rdof0 + k (rows of
-    // A), slot kMaxRowDofs + k holds DOF cdof0 + k (rows of B). Each K-block
-    // the CTA loads the next block's 16-byte chunks into registers first and
-    // stores them after building the current block, so the loads' latency
-    // hides behind the build.
-    unsigned char *binbuf = bin_buffer(smem);
-    constexpr int kLoads = kBinSlots * (kKB / 16);  // 16-byte chunks per K-block
-    auto load_chunk = [&](int L, int fbase, uint4 &v) -> bool {
-        const int slot = L >> 3, c = L & 7;
-        const int d = slot < kMaxRowDofs ? rdof0 + slot : cdof0 + slot - kMaxRowDofs;
-        const bool ok = slot < kMaxRowDofs ? d <= rlast : d <= clast;
-        if (ok) v = __ldg((const uint4 *)(bins + (int64_t)d * ldb + fbase + c * 16));
-        return ok;
-    };
-
-    // items: A rows 0..127 (1024 items), then B rows 0..511 (4096 items);
-    // item i -> (row group g, chunk c, row-in-group rr) with rr fastest, so
-    // 8 consecutive threads store one contiguous 128-B core matrix
-    constexpr int kItemsPerThread = (kM + kN) * (kKB / 16) / kThreads;  // 10
-    Item it[kItemsPerThread];
-#pragma unroll
-    for (int j = 0; j < kItemsPerThread; j++) {
-        const int i = tid + j * kThreads;
-        const bool isA = i < kM * 8;
-        const int ii = isA ? i : i - kM * 8;
-        const int rr = ii & 7, c = (ii >> 3) & 7, g = ii >> 6;
-        const int row = (isA ? r0 : c0) + g * 8 + rr;
-        it[j].dst = (isA ? 0u : (uint32_t)kAStage) + (uint32_t)((g * 8 + c) * 128 + rr * 16);
-        it[j].c16 = c * 16;
-        it[j].valid = row < R;
-        const uint32_t info = row < R ? rowinfo[row] : 0u;
-        const int d = (int)(info >> 8);
-        const int slot = isA ? d - rdof0 : kMaxRowDofs + d - cdof0;
-        it[j].soff = row < R ? (uint32_t)(slot * kKB + c * 16) : 0u;
-        it[j].t4 = (info & 0xffu) * 0x01010101u;
-    }
-
     const int nkb = (F + kKB - 1) / kKB;
-    const uint32_t sbase = smem_u32(stages);
-    // K-block 0's bin rows into buffer 0
-    for (int L = tid; L < kLoads; L += kThreads) {
-        uint4 v;
-        if (load_chunk(L, 0, v)) *(uint4 *)(binbuf + (L >> 3) * kKB + (L & 7) * 16) = v;
+    unsigned char *binbuf = bin_buffer(smem);  // [kBinBufs][kBinSlots][kKB]
+
+    if (warp == kLoaderWarp) {
+        // ------------------------------------------------------- MMA issuer
+        const uint32_t sbase = smem_u32(stages);
+        int kb = 0;
+        for (; kb < nkb; kb++) {
+            const int s = kb % kStages;
+            int ok = 1;
+            if (lane == 0) ok = mbar_wait_bounded(smem_u32(&full[s]), (uint32_t)((kb / kStages) & 1)) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok || s_abort) {
+                if (lane == 0) s_abort = 1;
+                break;
+            }
+            if (lane == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = sbase + s * kStageBytes, b0 = a0 + kAStage;
+#pragma unroll
+                for (int kk = 0; kk < kKB / 32; kk++) {
+#pragma unroll
+                    for (int h = 0; h < kN / kNH; h++) {  // B rows h*256.. start 32 row groups (32 KB) further
+                        mma_f8(tmem + h * kNH, smem_desc(a0 + kk * 256, 128, 1024),
+                               smem_desc(b0 + h * (kNH / 8) * 1024 + kk * 256, 128, 1024), (kb | kk) != 0);
+                    }
+                }
+                mma_commit(smem_u32(&empty[s]));
+            }
+            __syncwarp();
+        }
+        if (lane == 0) s_mma_issued = kb;
+    } else {
+        // ----------------------------------------------------------- builders
+        // items: A rows 0..127 (1024 items), then B rows 0..511 (4096 items);
+        // item i -> (row group g, chunk c, row-in-group rr) with rr fastest, so
+        // 8 consecutive threads store one contiguous 128-B core matrix
+        constexpr int kItems = (kM + kN) * (kKB / 16);
+        constexpr int kItemsPerThread = (kItems + kBuilders - 1) / kBuilders;  // 11
+        Item it[kItemsPerThread];
+#pragma unroll
+        for (int j = 0; j < kItemsPerThread; j++) {
+            const int i = tid + j * kBuilders;
+            const bool inr = i < kItems;
+            const bool isA = i < kM * 8;
+            const int ii = isA ? i : i - kM * 8;
+            const int rr = ii & 7, c = (ii >> 3) & 7, g = ii >> 6;
+            const int row = (isA ? r0 : c0) + g * 8 + rr;
+            it[j].dst = (isA ? 0u : (uint32_t)kAStage) + (uint32_t)((g * 8 + c) * 128 + rr * 16);
+            it[j].c16 = c * 16;
+            it[j].valid = inr && row < R;
+            const uint32_t info = it[j].valid ? rowinfo[row] : 0u;
+            const int d = (int)(info >> 8);
+            const int slot = isA ? d - rdof0 : kMaxRowDofs + d - cdof0;
+            it[j].soff = it[j].valid ? (uint32_t)(slot * kKB + c * 16) : 0u;
+            it[j].t4 = (info & 0xffu) * 0x01010101u;
+            if (!inr) it[j].dst = 0xffffffffu;  // no item
+        }
+        // Bin rows of K-block j go to ring buffer j % 4: slot k < kMaxRowDofs
+        // holds DOF rdof0 + k (rows of A), slot kMaxRowDofs + k holds DOF
+        // cdof0 + k (rows of B). Every builder thread loads its share of block
+        // kb + 2 into registers before building block kb and stores it after;
+        // the builders are never more than one block apart (the stage of
+        // block kb + 2 frees only when every builder finished block kb), so
+        // the buffer of block kb + 2 (last used by block kb - 2) is free.
+        constexpr int kLoads = kBinSlots * (kKB / 16);  // 16-byte chunks per K-block
+        constexpr int kLoadsPerThread = (kLoads + kBuilders - 1) / kBuilders;
+        auto load_chunk = [&](int L, int j, uint4 &v) -> bool {
+            const int slot = L >> 3, c = L & 7;
+            const int d = slot < kMaxRowDofs ? rdof0 + slot : cdof0 + slot - kMaxRowDofs;
+            const bool ok = L < kLoads && (slot < kMaxRowDofs ? d <= rlast : d <= clast);
+            if (ok) v = __ldg((const uint4 *)(bins + (int64_t)d * ldb + (int64_t)j * kKB + c * 16));
+            return ok;
+        };
+        auto store_block = [&](int j, const uint4 *v, const bool *ok) {
+            unsigned char *dst = binbuf + (j % kBinBufs) * kBinBufBytes;
+#pragma unroll
+            for (int q = 0; q < kLoadsPerThread; q++) {
+                const int L = tid + q * kBuilders;
+                if (ok[q]) *(uint4 *)(dst + (L >> 3) * kKB + (L & 7) * 16) = v[q];
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&binfull[j % kBinBufs]));
+        };
+        for (int j = 0; j < 2 && j < nkb; j++) {
+            uint4 v[kLoadsPerThread];
+            bool ok[kLoadsPerThread];
+#pragma unroll
+            for (int q = 0; q < kLoadsPerThread; q++) ok[q] = load_chunk(tid + q * kBuilders, j, v[q]);
+            store_block(j, v, ok);
+        }
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % kStages;
+            if (s_abort) break;
+            uint4 pf[kLoadsPerThread];
+            bool pv[kLoadsPerThread];
+#pragma unroll
+            for (int q = 0; q < kLoadsPerThread; q++)
+                pv[q] = kb + 2 < nkb ? load_chunk(tid + q * kBuilders, kb + 2, pf[q]) : false;
+            if (!mbar_wait_bounded(smem_u32(&binfull[kb % kBinBufs]), (uint32_t)((kb / kBinBufs) & 1)) ||
+                (kb >= kStages &&
+                 !mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)((kb / kStages - 1) & 1)))) {
+                s_abort = 1;
+                break;
+            }
+            const int nvalid = F - kb * kKB;  // frames of this block that exist (>= 1)
+            const unsigned char *bb = binbuf + (kb % kBinBufs) * kBinBufBytes;
+            unsigned char *st = stages + s * kStageBytes;
+#pragma unroll
+            for (int j = 0; j < kItemsPerThread; j++) {
+                if (it[j].dst == 0xffffffffu) continue;
+                uint4 o = make_uint4(0u, 0u, 0u, 0u);
+                if (it[j].valid) {
+                    const uint4 w = *(const uint4 *)(bb + it[j].soff);
+                    o.x = onehot4(w.x, it[j].t4);
+                    o.y = onehot4(w.y, it[j].t4);
+                    o.z = onehot4(w.z, it[j].t4);
+                    o.w = onehot4(w.w, it[j].t4);
+                    if (nvalid < kKB) {  // last block: frames past F are not data
+                        const int v = nvalid - it[j].c16;
+                        uint32_t m[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            const int bq = v - 4 * q;  // valid bytes in word q
+                            m[q] = bq >= 4 ? 0xffffffffu : (bq <= 0 ? 0u : (0xffffffffu >> (8 * (4 - bq))));
+                        }
+                        o.x &= m[0]; o.y &= m[1]; o.z &= m[2]; o.w &= m[3];
+                    }
+                }
+                *(uint4 *)(st + it[j].dst) = o;
+            }
+            // generic writes of the stage before the tensor core reads it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[s]));
+            if (kb + 2 < nkb) store_block(kb + 2, pf, pv);
+        }
     }
     __syncthreads();
 
-    bool aborted = false;  // uniform over the CTA (set from __syncthreads_or)
-    for (int kb = 0; kb < nkb; kb++) {
-        const int s = kb % kStages;
-        if (kb >= kStages) {  // stage s is free once the MMAs of block kb - kStages completed
-            const bool ok = mbar_wait_bounded(smem_u32(&mma_done[s]), (uint32_t)((kb / kStages - 1) & 1));
-            if (__syncthreads_or(!ok)) {
-                aborted = true;
-                break;
-            }
-        }
-        const int fbase = kb * kKB;
-        const int nvalid = F - fbase;  // frames of this block that exist (>= 1)
-        // prefetch the next block's bin rows into registers
-        uint4 pf[2];
-        bool pv[2] = {false, false};
-        if (kb + 1 < nkb) {
-#pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const int L = tid + q * kThreads;
-                if (L < kLoads) pv[q] = load_chunk(L, fbase + kKB, pf[q]);
-            }
-        }
-        const unsigned char *bb = binbuf + (kb & 1) * kBinBufBytes;
-        unsigned char *st = stages + s * kStageBytes;
-#pragma unroll
-        for (int j = 0; j < kItemsPerThread; j++) {
-            uint4 o = make_uint4(0u, 0u, 0u, 0u);
-            if (it[j].valid) {
-                const uint4 w = *(const uint4 *)(bb + it[j].soff);
-                o.x = onehot4(w.x, it[j].t4);
-                o.y = onehot4(w.y, it[j].t4);
-                o.z = onehot4(w.z, it[j].t4);
-                o.w = onehot4(w.w, it[j].t4);
-                if (nvalid < kKB) {  // last block: frames past F are not data
-                    const int v = nvalid - it[j].c16;
-                    uint32_t m[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int bq = v - 4 * q;  // valid bytes in word q
-                        m[q] = bq >= 4 ? 0xffffffffu : (bq <= 0 ? 0u : (0xffffffffu >> (8 * (4 - bq))));
-                    }
-                    o.x &= m[0]; o.y &= m[1]; o.z &= m[2]; o.w &= m[3];
-                }
-            }
-            *(uint4 *)(st + it[j].dst) = o;
-        }
-        // the other buffer was last read while building block kb-1 (before the
-        // previous barrier): it can take the prefetched rows now
-#pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const int L = tid + q * kThreads;
-            if (pv[q]) *(uint4 *)(binbuf + ((kb + 1) & 1) * kBinBufBytes + (L >> 3) * kKB + (L & 7) * 16) = pf[q];
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core reads
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = sbase + s * kStageBytes, b0 = a0 + kAStage;
-#pragma unroll
-            for (int kk = 0; kk < kKB / 32; kk++) {
-#pragma unroll
-                for (int h = 0; h < kN / kNH; h++) {  // B rows h*256.. start 32 row groups (32 KB) further
-                    mma_f8(tmem + h * kNH, smem_desc(a0 + kk * 256, 128, 1024),
-                           smem_desc(b0 + h * (kNH / 8) * 1024 + kk * 256, 128, 1024), (kb | kk) != 0);
-                }
-            }
-            mma_commit(smem_u32(&mma_done[s]));
-        }
-    }
-
-    // wait for the last MMAs (the commit of the final block covers all earlier ones)
-    if (!aborted && nkb > 0) {
-        const int last = nkb - 1, s = last % kStages;
-        const bool ok = mbar_wait_bounded(smem_u32(&mma_done[s]), (uint32_t)((last / kStages) & 1));
-        if (__syncthreads_or(!ok)) aborted = true;
+    bool aborted = s_abort != 0;
+    if (!aborted && nkb > 0) {  // the commit of the final block covers every earlier MMA
+        const int last = nkb - 1;
+        if (!mbar_wait_bounded(smem_u32(&empty[last % kStages]), (uint32_t)((last / kStages) & 1))) s_abort = 1;
+        aborted = __syncthreads_or(s_abort != 0);
     }
     if (aborted) {
+        // a wait ran out: record it, let issued MMAs finish (bounded), free
+        // the tensor memory and leave
         if (tid == 0) {
             atomicAdd(&err[ERR_TIMEOUT], 1);
-            for (int s = 0; s < kStages; s++) (void)mbar_wait_bounded(smem_u32(&mma_done[s]), 0u);
+            const int nm = s_mma_issued;
+            for (int k = nm > kStages ? nm - kStages : 0; k < nm; k++)
+                (void)mbar_wait_bounded(smem_u32(&empty[k % kStages]), (uint32_t)((k / kStages) & 1));
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -496,13 +546,13 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
 // Form choice, from measured GB300 pair-kernel times at 2,994 DOFs x 100,000
 // frames: the histogram form takes 85.6 ms at any bin count up to 32 (32-slot
 // layout, one conflict-free shared-memory reduction per update) and 117.6 ms
-// from 36 to 50 (16-slot layout); the one-hot form takes 41.8 / 53.7 / 65.2 /
-// 79.1 / 92.9 ms at 8 / 9 / 10 / 11 / 12 bins (B1*B2 FP8 MACs per update, so
-// its time grows as B^2). The one-hot form wins up to 11 bins.
+// from 36 to 50 (16-slot layout); the one-hot form takes 34.9 / 45.1 / 54.6 /
+// 66.7 / 78.0 / 104.0 ms at 8 / 9 / 10 / 11 / 12 / 14 bins (B1*B2 FP8 MACs per
+// update, so its time grows as B^2). The one-hot form wins up to 12 bins.
 int autotune_form(const SysGeom &g) {
     int bmax = 0;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (pairs_onehot_supported(g) && bmax <= 11 && g.F >= 4096) return PG_FORM_ONEHOT;
+    if (pairs_onehot_supported(g) && bmax <= 12 && g.F >= 4096) return PG_FORM_ONEHOT;
     return PG_FORM_HIST;
 }
 
