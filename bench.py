@@ -110,6 +110,9 @@ def parse():
                     help="atoms of the bounded DOF sample timed on the host cores "
                          "(0: sized to ~2.5e10 pair-frame updates, about 10 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ingest", action="store_true",
+                    help="instead of the step: write the workload as a .bat (under $TMPDIR) and time "
+                         "pg_bat_read (host columns) against pg_bat_read_device (device columns)")
     return ap.parse_args()
 
 
@@ -592,8 +595,50 @@ def run_gb300(args):
     return 0
 
 
+def run_ingest(args):
+    """.bat ingest throughput: the workload written once as a .bat file, then
+    read `steps` times by each reader (after `warmup` untimed reads, so the
+    file is in the page cache for both). Prints one JSON line."""
+    import shutil
+
+    import parent_gb300 as pg
+    n_atoms, F, prec, fbd, fbb, lat = WORKLOADS[args.workload]
+    t = pg.synth_host(n_atoms, F, double_prec=prec, seed=20260, n_latents=lat, frac_bimodal_dih=fbd,
+                      frac_bimodal_bond=fbb)
+    d = Path(tempfile.mkdtemp(prefix="pg_ingest_"))
+    try:
+        path = d / "traj.bat"
+        t0 = time.perf_counter()
+        pg.write_bat(path, t)
+        write_s = time.perf_counter() - t0
+        del t
+        size = path.stat().st_size
+        res = {}
+        for name, dev in (("host", None), ("device", 0)):
+            times = []
+            for k in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                b = pg.BatFile(path, device=dev)
+                dt = time.perf_counter() - t0
+                b.close()
+                if k >= args.warmup:
+                    times.append(dt)
+            s = statistics.median(times)
+            res[name] = {"s": round(s, 4), "GB_per_s": round(size / s / 1e9, 2), "runs": [round(x, 4) for x in times]}
+        print(json.dumps({"metric": ".bat ingest (file -> DOF-major columns)", "file_bytes": size,
+                          "write_s": round(write_s, 2), "host_reader": res["host"], "device_reader": res["device"],
+                          "reader_threads": min(16, os.cpu_count() or 1), "page_cache": "warm",
+                          "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F,
+                                     "input": "fp64" if prec else "fp32"}}), flush=True)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.ingest:
+        return run_ingest(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -209,6 +209,13 @@ PG_API int pg_dof_stats(pg_ctx *ctx, double *mn, double *mx, double *shift);
  * to DOF-major scatter (PARENT.cpp:443-473). */
 typedef struct pg_bat pg_bat;
 PG_API int pg_bat_read(const char *path, pg_bat **out);
+/* Same file, same checks and messages, but the columns end up in device
+ * memory on `device` (owned by the pg_bat, freed by pg_bat_free): the frame
+ * records are read in large chunks by several threads into pinned buffers,
+ * copied up unchanged and transposed by a kernel while the next chunk is
+ * read. The view (pg_bat_view_of) then has on_device = 1 and ld = n_frames
+ * rounded up to 32. */
+PG_API int pg_bat_read_device(const char *path, int device, pg_bat **out);
 PG_API void pg_bat_free(pg_bat *bat);
 PG_API int pg_bat_view_of(const pg_bat *bat, pg_bat_view *view);
 PG_API int pg_bat_n_dihedrals(const pg_bat *bat);

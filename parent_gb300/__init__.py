@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
                                C.POINTER(C.c_int), C.POINTER(C.c_int64), i64]),
         "pg_dof_stats": (i, [vp, dp, dp, dp]),
         "pg_bat_read": (i, [cp, C.POINTER(vp)]),
+        "pg_bat_read_device": (i, [cp, i, C.POINTER(vp)]),
         "pg_bat_free": (None, [vp]),
         "pg_bat_view_of": (i, [vp, C.POINTER(BatView)]),
         "pg_bat_n_dihedrals": (i, [vp]),
@@ -385,11 +386,16 @@ class Engine:
 # ----------------------------------------------------------------- files
 
 class BatFile:
-    """A .bat read by pg_bat_read (header + DOF-major columns in pinned memory)."""
+    """A .bat: header + DOF-major columns, read by pg_bat_read into pinned host
+    memory, or with device=<index> by pg_bat_read_device into device memory
+    (records streamed up and transposed on the GPU)."""
 
-    def __init__(self, path: str | Path):
+    def __init__(self, path: str | Path, device: int | None = None):
         self._h = C.c_void_p()
-        _check(lib().pg_bat_read(str(path).encode(), C.byref(self._h)))
+        if device is None:
+            _check(lib().pg_bat_read(str(path).encode(), C.byref(self._h)))
+        else:
+            _check(lib().pg_bat_read_device(str(path).encode(), int(device), C.byref(self._h)))
 
     def view(self) -> BatView:
         v = BatView()

@@ -40,6 +40,7 @@ CU_SOURCES = {
     "pg_mist.cu": [],
     "pg_synth.cu": [],
     "pg_noalloc.cu": [],
+    "pg_ingest.cu": [],
 }
 CPP_SOURCES = ["pg_io.cpp"]
 CLIS = ["PARENT_gb300", "get_PAR_MIST_gb300", "get_PAR_MIE_gb300", "get_PAR_info_gb300"]

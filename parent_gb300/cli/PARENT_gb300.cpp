@@ -9,6 +9,9 @@
 // shard. Shard sums are exact, so the .par is identical to a one-pass run.
 // PG_STOP_AFTER_SHARDS=n ends the run (exit code 3) after n shards of this
 // invocation, to exercise the resume path.
+//
+// The .bat columns are read straight into device memory (pg_bat_read_device);
+// PG_BAT_READ=host reads them into pinned host memory instead.
 #include <stdint.h>
 #include <stdio.h>
 #include <sys/stat.h>
@@ -101,7 +104,11 @@ int main(int argc, char **argv) {
     }
     printf("Reading file %s .\n", argv[1]);
     pg_bat *bat = nullptr;
-    if (pg_bat_read(argv[1], &bat) != PG_OK) {
+    // the columns go straight to the device (records streamed up and
+    // transposed there); PG_BAT_READ=host transposes on the host instead
+    const char *eread = getenv("PG_BAT_READ");
+    const bool host_read = eread && strcmp(eread, "host") == 0;
+    if ((host_read ? pg_bat_read(argv[1], &bat) : pg_bat_read_device(argv[1], env_device(), &bat)) != PG_OK) {
         fprintf(stderr, "AN ERROR HAS OCCURED WHILE READING THE HEADER OF THE FILE %s . QUITTING PROGRAM.\n", argv[1]);
         return 1;
     }

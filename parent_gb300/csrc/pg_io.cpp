@@ -5,16 +5,21 @@
 //         read_PAR_header / read_PAR_body    (io_binary.cpp:446-673)
 //   text  get_PAR_MIE (get_PAR_MIE.cpp:109-199), get_PAR_MIST (get_PAR_MIST.cpp:667-765),
 //         get_PAR_info (get_PAR_info.cpp:64-79)
-// The .bat body is frame-major; it is transposed here into DOF-major columns
-// kept in the file's own precision (pinned host memory), which is the layout
-// the device kernels read.
+// The .bat body is frame-major; it is transposed into DOF-major columns kept
+// in the file's own precision, which is the layout the device kernels read:
+// on the host (pg_bat_read, pinned memory) or on the device (pg_bat_read_device:
+// raw records are streamed up and transposed by a kernel).
 #include <cuda_runtime.h>
+#include <errno.h>
+#include <fcntl.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <thread>
 #include <vector>
@@ -27,6 +32,8 @@ namespace {
 
 namespace pg {
 void set_global_error(const char *msg);
+cudaError_t launch_bat_transpose(const uint8_t *raw, int nf, int64_t rec, int off0, int es, int n_dih,
+                                 uint8_t *cols, int64_t ld, int64_t f0, cudaStream_t st);
 }
 
 namespace {
@@ -121,8 +128,10 @@ void synthetic_header(Header &h) {
 
 struct pg_bat {
     Header h;
-    void *cols = nullptr;  // pinned, DOF-major, bonds | angles | dihedrals
+    void *cols = nullptr;  // DOF-major, bonds | angles | dihedrals; host (pinned or not) or device
     bool pinned = false;
+    int device = -1;       // >= 0: cols is device memory on this device
+    int64_t ld = 0;        // elements between columns
     size_t bytes = 0;
 };
 
@@ -142,6 +151,80 @@ static void layout(int nd_, int64_t off[10]) {
 
 extern "C" {
 
+// Reads the .bat header (read_BAT_header, io_binary.cpp:107-200) with its
+// checks; leaves `f` at the first frame record.
+static int read_bat_header(FILE *f, Header &h, const char *path) {
+    if (!rd(f, &h.version, 4) || !rd(f, &h.double_prec, 4) || !rd(f, &h.n_dih, 4) || !rd(f, &h.n_frames, 4))
+        return ioerr(PG_ERR_IO, "ERROR: could not read the header of %s", path);
+    // the checks of read_BAT_header, io_binary.cpp:127-145
+    if (h.version < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version);
+    if (h.double_prec != 0 && h.double_prec != 1)
+        return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!",
+                     h.double_prec);
+    if (h.n_dih > 19997)
+        fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n",
+                h.n_dih + 3);
+    if (h.n_dih < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih);
+    if (h.n_frames < 1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames);
+    if (h.version >= 3) {
+        if (!read_atoms(f, h)) return ioerr(PG_ERR_IO, "ERROR: truncated atom block in %s", path);
+    } else {
+        synthetic_header(h);  // pre-3 files carry no atom names
+    }
+    h.dih.resize((size_t)6 * h.n_dih);
+    h.masses.resize((size_t)h.n_dih + 3);
+    if ((h.n_dih && !rd(f, h.dih.data(), h.dih.size() * 4)) || !rd(f, h.masses.data(), h.masses.size() * 4))
+        return ioerr(PG_ERR_IO, "ERROR: truncated dihedral/mass block in %s", path);
+    return PG_OK;
+}
+
+static int reader_threads() { return (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency())); }
+
+// Reads `bytes` at file offset `off` into dst with up to `nth` threads
+// (positioned reads, so the slices share no file offset). False on a short
+// read.
+static bool pread_all(int fd, int64_t off, unsigned char *dst, size_t bytes, int nth) {
+    const size_t slice = std::max<size_t>((size_t)4 << 20, (bytes + nth - 1) / nth);
+    std::atomic<bool> ok{true};
+    auto work = [&](size_t a, size_t b) {
+        while (a < b) {
+            const ssize_t n = pread(fd, dst + a, b - a, (off_t)(off + (int64_t)a));
+            if (n < 0 && errno == EINTR) continue;
+            if (n <= 0) {
+                ok = false;
+                return;
+            }
+            a += (size_t)n;
+        }
+    };
+    std::vector<std::thread> th;
+    for (size_t a = slice; a < bytes; a += slice) th.emplace_back(work, a, std::min(bytes, a + slice));
+    work(0, std::min(bytes, slice));
+    for (auto &t : th) t.join();
+    return ok;
+}
+
+// Frame records: 11 floats (44 bytes), 6 root externals, b0 b1 a0, then
+// (b, a, d) per dihedral (read_BAT_frame, io_binary.cpp:281-368).
+static size_t record_bytes(const Header &h) { return 44 + (size_t)(9 + 3 * h.n_dih) * (h.double_prec ? 8 : 4); }
+static int record_values_offset(const Header &h) { return 44 + 6 * (h.double_prec ? 8 : 4); }
+
+// Column of value u of a record (u counted from b0): bonds | angles | dihedrals.
+static size_t column_of_value(int u, int nb, int na) {
+    if (u < 2) return (size_t)u;
+    if (u == 2) return (size_t)nb;
+    const int k = (u - 3) / 3, r = (u - 3) - 3 * k;
+    return r == 0 ? (size_t)k + 2 : (r == 1 ? (size_t)nb + k + 1 : (size_t)nb + na + k);
+}
+
+static size_t chunk_bytes_setting() {
+    if (const char *e = getenv("PG_BAT_CHUNK_BYTES")) {
+        const long long v = atoll(e);
+        if (v > 0) return (size_t)v;
+    }
+    return (size_t)64 << 20;
+}
+
 PG_API int pg_bat_read(const char *path, pg_bat **out) {
     if (!path || !out) return ioerr(PG_ERR_ARG, "pg_bat_read: null argument");
     *out = nullptr;
@@ -149,35 +232,14 @@ PG_API int pg_bat_read(const char *path, pg_bat **out) {
     if (!f) return ioerr(PG_ERR_IO, "ERROR: Could not open file %s !", path);
     pg_bat *b = new pg_bat;
     Header &h = b->h;
-    int rc = PG_OK;
+    int rc = read_bat_header(f, h, path);
     do {
-        if (!rd(f, &h.version, 4) || !rd(f, &h.double_prec, 4) || !rd(f, &h.n_dih, 4) || !rd(f, &h.n_frames, 4)) {
-            rc = ioerr(PG_ERR_IO, "ERROR: could not read the header of %s", path);
-            break;
-        }
-        // the checks of read_BAT_header, io_binary.cpp:127-145
-        if (h.version < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version); break; }
-        if (h.double_prec != 0 && h.double_prec != 1) {
-            rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!", h.double_prec);
-            break;
-        }
-        if (h.n_dih > 19997) fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n", h.n_dih + 3);
-        if (h.n_dih < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih); break; }
-        if (h.n_frames < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames); break; }
-        if (h.version >= 3) {
-            if (!read_atoms(f, h)) { rc = ioerr(PG_ERR_IO, "ERROR: truncated atom block in %s", path); break; }
-        } else {
-            synthetic_header(h);  // pre-3 files carry no atom names
-        }
-        h.dih.resize((size_t)6 * h.n_dih);
-        h.masses.resize((size_t)h.n_dih + 3);
-        if ((h.n_dih && !rd(f, h.dih.data(), h.dih.size() * 4)) || !rd(f, h.masses.data(), h.masses.size() * 4)) {
-            rc = ioerr(PG_ERR_IO, "ERROR: truncated dihedral/mass block in %s", path);
-            break;
-        }
+        if (rc != PG_OK) break;
+        const int64_t body = (int64_t)ftell(f);
         const int nb = h.n_dih + 2, na = h.n_dih + 1, nd = h.n_dih;
         const size_t F = (size_t)h.n_frames, es = h.double_prec ? 8 : 4;
         const size_t D = (size_t)nb + na + nd;
+        b->ld = (int64_t)F;
         b->bytes = D * F * es;
         if (cudaHostAlloc(&b->cols, b->bytes, cudaHostAllocDefault) == cudaSuccess) {
             b->pinned = true;
@@ -186,37 +248,33 @@ PG_API int pg_bat_read(const char *path, pg_bat **out) {
             b->cols = malloc(b->bytes);
             if (!b->cols) { rc = ioerr(PG_ERR_NOMEM, "ERROR ALLOCATNG MEMORY! (%zu bytes)", b->bytes); break; }
         }
-        // frames: 11 floats, 6 externals, b0 b1 a0, then (b, a, d) per dihedral
-        const size_t fbytes = 44 + (size_t)(9 + 3 * nd) * es;
-        const size_t batch = std::max<size_t>(1, (64u << 20) / fbytes);
-        std::vector<unsigned char> buf(batch * fbytes);
+        const size_t rec = record_bytes(h), off0 = (size_t)record_values_offset(h);
+        const size_t batch = std::max<size_t>(1, chunk_bytes_setting() / rec);
+        std::vector<unsigned char> buf(batch * rec);
         unsigned char *cols = (unsigned char *)b->cols;
-        unsigned char *B = cols, *A = cols + (size_t)nb * F * es, *Dd = A + (size_t)na * F * es;
+        const int nth = reader_threads(), nvals = 3 + 3 * nd;
         for (size_t f0 = 0; f0 < F && rc == PG_OK; f0 += batch) {
             const size_t nf = std::min(batch, F - f0);
-            if (!rd(f, buf.data(), nf * fbytes)) {
+            if (!pread_all(fileno(f), body + (int64_t)(f0 * rec), buf.data(), nf * rec, nth)) {
                 rc = ioerr(PG_ERR_IO, "An ERROR has occurred while reading the file %s . (frame %zu)", path, f0);
                 break;
             }
-            // transpose the batch with a few threads (columns are disjoint)
-            const int nth = (int)std::min<size_t>(8, std::max<size_t>(1, nf / 256));
+            // transpose: each thread owns a range of values (columns), and
+            // walks 64-frame blocks so every column is written in runs
+            const int nt = std::min(nth, std::max(1, nvals / 32));
             auto work = [&](int t) {
-                for (size_t i = t; i < nf; i += nth) {
-                    const unsigned char *p = buf.data() + i * fbytes + 44 + 6 * es;
-                    const size_t fr = f0 + i;
-                    memcpy(B + fr * es, p, es);
-                    memcpy(B + (F + fr) * es, p + es, es);
-                    memcpy(A + fr * es, p + 2 * es, es);
-                    p += 3 * es;
-                    for (int d = 0; d < nd; d++, p += 3 * es) {
-                        memcpy(B + ((size_t)(d + 2) * F + fr) * es, p, es);
-                        memcpy(A + ((size_t)(d + 1) * F + fr) * es, p + es, es);
-                        memcpy(Dd + ((size_t)d * F + fr) * es, p + 2 * es, es);
+                const int ua = (int)((int64_t)nvals * t / nt), ub = (int)((int64_t)nvals * (t + 1) / nt);
+                for (size_t i0 = 0; i0 < nf; i0 += 64) {
+                    const size_t i1 = std::min(nf, i0 + 64);
+                    for (int u = ua; u < ub; u++) {
+                        unsigned char *dst = cols + (column_of_value(u, nb, na) * F + f0) * es;
+                        const unsigned char *src = buf.data() + off0 + (size_t)u * es;
+                        for (size_t i = i0; i < i1; i++) memcpy(dst + i * es, src + i * rec, es);
                     }
                 }
             };
             std::vector<std::thread> th;
-            for (int t = 1; t < nth; t++) th.emplace_back(work, t);
+            for (int t = 1; t < nt; t++) th.emplace_back(work, t);
             work(0);
             for (auto &x : th) x.join();
         }
@@ -230,26 +288,129 @@ PG_API int pg_bat_read(const char *path, pg_bat **out) {
     return PG_OK;
 }
 
+PG_API int pg_bat_read_device(const char *path, int device, pg_bat **out) {
+    if (!path || !out) return ioerr(PG_ERR_ARG, "pg_bat_read_device: null argument");
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: Could not open file %s !", path);
+    pg_bat *b = new pg_bat;
+    Header &h = b->h;
+    int rc = read_bat_header(f, h, path);
+    const int64_t body = rc == PG_OK ? (int64_t)ftell(f) : 0;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    const int nst = 3;  // staging ring: read chunk k+1 while chunk k is copied and transposed
+    unsigned char *pin[nst] = {nullptr, nullptr, nullptr}, *raw[nst] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev[nst] = {nullptr, nullptr, nullptr};
+    cudaStream_t st = nullptr;
+    auto cuda_fail = [&](cudaError_t e, const char *what) {
+        cudaGetLastError();
+        return ioerr(e == cudaErrorMemoryAllocation ? PG_ERR_NOMEM : PG_ERR_CUDA, "ERROR: %s (%s) while reading %s",
+                     what, cudaGetErrorString(e), path);
+    };
+    do {
+        if (rc != PG_OK) break;
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "cudaSetDevice"); break; }
+        b->device = device;
+        const int nb = h.n_dih + 2, na = h.n_dih + 1, nd = h.n_dih;
+        const size_t F = (size_t)h.n_frames, es = h.double_prec ? 8 : 4;
+        const size_t D = (size_t)nb + na + nd;
+        b->ld = (int64_t)((F + 31) / 32 * 32);
+        b->bytes = D * (size_t)b->ld * es;
+        if ((e = cudaMalloc(&b->cols, b->bytes)) != cudaSuccess) {
+            b->cols = nullptr;
+            rc = cuda_fail(e, "device allocation of the columns");
+            break;
+        }
+        const size_t rec = record_bytes(h);
+        const int off0 = record_values_offset(h);
+        size_t nfc = std::max<size_t>(32, chunk_bytes_setting() / rec / 32 * 32);
+        nfc = std::min(nfc, (F + 31) / 32 * 32);
+        for (int k = 0; k < nst && rc == PG_OK; k++) {
+            if ((e = cudaHostAlloc(&pin[k], nfc * rec, cudaHostAllocDefault)) != cudaSuccess) pin[k] = nullptr;
+            else if ((e = cudaMalloc(&raw[k], nfc * rec)) != cudaSuccess) raw[k] = nullptr;
+            else e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+            if (e != cudaSuccess) rc = cuda_fail(e, "staging buffers");
+        }
+        if (rc != PG_OK) break;
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) {
+            st = nullptr;
+            rc = cuda_fail(e, "cudaStreamCreate");
+            break;
+        }
+        const int nth = reader_threads();
+        size_t c = 0;
+        for (size_t f0 = 0; f0 < F; f0 += nfc, c++) {
+            const int k = (int)(c % nst);
+            if (c >= (size_t)nst && (e = cudaEventSynchronize(ev[k])) != cudaSuccess) {
+                rc = cuda_fail(e, "staging");
+                break;
+            }
+            const size_t nf = std::min(nfc, F - f0);
+            if (!pread_all(fileno(f), body + (int64_t)(f0 * rec), pin[k], nf * rec, nth)) {
+                rc = ioerr(PG_ERR_IO, "An ERROR has occurred while reading the file %s . (frame %zu)", path, f0);
+                break;
+            }
+            if ((e = cudaMemcpyAsync(raw[k], pin[k], nf * rec, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+                (e = pg::launch_bat_transpose(raw[k], (int)nf, (int64_t)rec, off0, (int)es, nd,
+                                              (uint8_t *)b->cols, b->ld, (int64_t)f0, st)) != cudaSuccess ||
+                (e = cudaEventRecord(ev[k], st)) != cudaSuccess) {
+                rc = cuda_fail(e, "upload");
+                break;
+            }
+        }
+        if (st) {
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess && rc == PG_OK) rc = cuda_fail(e, "transpose");
+        }
+    } while (0);
+    fclose(f);
+    if (st) cudaStreamDestroy(st);
+    for (int k = 0; k < nst; k++) {
+        if (ev[k]) cudaEventDestroy(ev[k]);
+        if (raw[k]) cudaFree(raw[k]);
+        if (pin[k]) cudaFreeHost(pin[k]);
+    }
+    cudaSetDevice(prev);
+    if (rc != PG_OK) {
+        pg_bat_free(b);
+        return rc;
+    }
+    *out = b;
+    return PG_OK;
+}
+
 PG_API void pg_bat_free(pg_bat *b) {
     if (!b) return;
     if (b->cols) {
-        if (b->pinned) cudaFreeHost(b->cols); else free(b->cols);
+        if (b->device >= 0) {
+            int prev = 0;
+            cudaGetDevice(&prev);
+            cudaSetDevice(b->device);
+            cudaFree(b->cols);
+            cudaSetDevice(prev);
+        } else if (b->pinned) {
+            cudaFreeHost(b->cols);
+        } else {
+            free(b->cols);
+        }
     }
     delete b;
 }
 
 PG_API int pg_bat_view_of(const pg_bat *b, pg_bat_view *v) {
     if (!b || !v) return PG_ERR_ARG;
-    const size_t F = (size_t)b->h.n_frames, es = b->h.double_prec ? 8 : 4;
+    const size_t ld = (size_t)b->ld, es = b->h.double_prec ? 8 : 4;
     const int nb = b->h.n_dih + 2, na = b->h.n_dih + 1;
     v->n_dihedrals = b->h.n_dih;
     v->n_frames = b->h.n_frames;
     v->double_prec = b->h.double_prec;
-    v->on_device = 0;
-    v->ld = (int64_t)F;
+    v->on_device = b->device >= 0 ? 1 : 0;
+    v->ld = (int64_t)ld;
     v->bonds = b->cols;
-    v->angles = (const char *)b->cols + (size_t)nb * F * es;
-    v->dihedrals = (const char *)b->cols + (size_t)(nb + na) * F * es;
+    v->angles = (const char *)b->cols + (size_t)nb * ld * es;
+    v->dihedrals = (const char *)b->cols + (size_t)(nb + na) * ld * es;
     return PG_OK;
 }
 PG_API int pg_bat_n_dihedrals(const pg_bat *b) { return b ? b->h.n_dih : -1; }
