@@ -156,6 +156,8 @@ static DofArrays dof_arrays(pg_ctx *ctx, int D) {
 static size_t elem_size(int prec) { return prec ? 8 : 4; }
 
 // Validation and the geometry of a trajectory (ctx->geo).
+static bool needs_row_codes(const SysGeom &g);
+
 static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     if (!tv || !bins) return fail(ctx, PG_ERR_ARG, "null trajectory or bins");
     if (tv->n_dihedrals < 0 || tv->n_frames < 1)
@@ -181,6 +183,8 @@ static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6])
     g.F = tv->n_frames;
     g.ldb = bins_ld(g.F);
     for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
+    g.codes = 0;
+    g.codes = needs_row_codes(g) ? 1 : 0;
     ctx->resident = false;
     return PG_OK;
 }
@@ -226,7 +230,7 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
     }
     CK(cudaEventRecord(ctx->ev[1], st));
 
-    CK(ctx->bins.ensure((size_t)D * g.ldb));
+    CK(ctx->bins.ensure(bins_bytes(g)));
     CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
     CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
@@ -293,14 +297,17 @@ static int ensure_fix_table(pg_ctx *ctx, int F) {
 // Histogram layout, from measured inner-loop rates: the 32-slot kernel with
 // 32-bit counters (one wavefront per warp-wide reduction) for 2D bin counts
 // up to 35; the 16-slot kernel (two lanes per pair) above that, where the
-// 32-slot kernel needs 16-bit counters and runs slower. PG_HIST_SLOTS=16 or
-// 32 forces one layout (32 slots up to 50 bins).
+// 32-slot kernel needs 16-bit counters. PG_HIST_SLOTS=16 or 32 forces one
+// layout (32 slots up to 50 bins).
 static bool use_hist32(const SysGeom &g) {
     const char *e = getenv("PG_HIST_SLOTS");
     if (e && atoi(e) == 16) return false;
     if (e && atoi(e) == 32) return pairs_hist32_supported(bmax_of(g));
     return pairs_hist32_wide(bmax_of(g));
 }
+
+// The 16-bit 32-slot layout stages its row DOFs from the row-code matrix.
+static bool needs_row_codes(const SysGeom &g) { return use_hist32(g) && !pairs_hist32_wide(bmax_of(g)); }
 
 // Launches the 32-slot kernel over the cached full tile list (explicit ==
 // nullptr) or over n_explicit given tiles; the per-CTA accumulators live in
@@ -379,7 +386,7 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
     if (prep_smem_bytes(g) > 200 * 1024) return fail(ctx, PG_ERR_UNSUPPORTED, "1D bin counts too large");
     const ParLayout L = par_layout(g.n_dih);
     CK(ctx->cols.ensure((size_t)D * F * es + 256));
-    CK(ctx->bins.ensure((size_t)D * g.ldb));
+    CK(ctx->bins.ensure(bins_bytes(g)));
     CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
     CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
@@ -1029,6 +1036,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         g.F = v.n_frames;
         g.ldb = bins_ld(g.F);
         for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
+        g.codes = 0;
+        g.codes = needs_row_codes(g) ? 1 : 0;
         L.prec = v.double_prec;
         L.own_cols = !v.on_device;
         L.ld = v.on_device ? v.ld : v.n_frames;
@@ -1037,7 +1046,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
             off = al256(off + (size_t)g.D * g.F * elem_size(v.double_prec));
         }
         L.bins = off;
-        off = al256(off + (size_t)g.D * g.ldb);
+        off = al256(off + bins_bytes(g));
         L.dof = off;
         off = al256(off + (size_t)g.D * (5 * sizeof(double) + 2 * sizeof(int)) + 64);
         L.par = off;
@@ -1158,6 +1167,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     }
     key.push_back((int64_t)ctx->nfix_max);
     key.push_back(h32 ? (int64_t)(uintptr_t)ctx->scratch.p : -1);
+    key.push_back(sys[0].g.codes);
     for (int k = 0; k < 6; k++) key.push_back(bins[k]);
     for (int s = 0; s < n_sys; s++) {
         const pg_bat_view &v = trajs[s];
@@ -1215,7 +1225,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
                                 st);
         }
         if (e == cudaSuccess)
-            e = h32 ? launch_pairs_hist32_batch(bmax, (const SysDesc *)(meta + mo_sd), (const PairTile *)(meta + mo_t),
+            e = h32 ? launch_pairs_hist32_batch(bmax, sys[0].g.codes != 0, (const SysDesc *)(meta + mo_sd),
+                                                (const PairTile *)(meta + mo_t),
                                                 (const int *)(meta + mo_ts), (int64_t)tiles.size(),
                                                 (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,
                                                 (int *)ctx->errw.p, ctx->scratch.p, sb32, st)

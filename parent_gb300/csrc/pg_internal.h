@@ -28,7 +28,12 @@ struct SysGeom {
     int F;                     // frames
     int64_t ldb;               // bytes between DOF rows of the uint8 bin matrix (bins_ld(F))
     int bins[6];               // b1D a1D d1D b2D a2D d2D
+    int codes;                 // 1: a second D x ldb matrix follows the bin matrix, holding
+                               // each 2D bin b as the row code (b >> 1) | (b & 1) << 7
 };
+
+// Bytes of the bin matrix (and the row-code matrix after it, if any).
+inline size_t bins_bytes(const SysGeom &g) { return (size_t)g.D * (size_t)g.ldb * (g.codes ? 2 : 1); }
 
 __host__ __device__ inline int dof_type(int g, int nb, int na) {
     return g < nb ? TB : (g < nb + na ? TA : TD);
@@ -149,11 +154,12 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
 // staging geometry (frames per chunk, stages).
 int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages);
 
-// 32-slot histogram pair kernel (2D bins <= 50): 16-bit conflict-free
-// counters over 4 x 8-DOF tiles, persistent grid of pairs_hist32_grid(n)
-// CTAs; tiles that could overflow a 16-bit counter move counts into a per-CTA
-// overflow area in `scratch` (pairs_hist32_scratch_bytes, zeroed by the
-// launcher) every 32,768 frames.
+// 32-slot histogram pair kernel (2D bins <= 50): conflict-free counters over
+// 4 x 8-DOF tiles, persistent grid of pairs_hist32_grid(n) CTAs. Up to 35
+// bins 32-bit counters; 36-50 bins 16-bit counters, which need the row-code
+// matrix (SysGeom::codes), and tiles that could overflow a 16-bit counter move
+// counts into a per-CTA overflow area in `scratch`
+// (pairs_hist32_scratch_bytes, zeroed by the launcher) every 32,768 frames.
 bool pairs_hist32_supported(int bmax);
 bool pairs_hist32_wide(int bmax);  // 32-bit counters fit (2D bins <= 35)
 int pairs_hist32_grid(int64_t n_tiles);
@@ -161,9 +167,9 @@ size_t pairs_hist32_scratch_bytes(int bmax, int grid);
 cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
                                 PairOut out, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
-cudaError_t launch_pairs_hist32_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
-                                      int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
-                                      void *scratch, size_t scratch_bytes, cudaStream_t st);
+cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, const PairTile *tiles,
+                                      const int *tile_sys, int64_t n_tiles, const unsigned long long *nfix,
+                                      double fix, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
 
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,

@@ -12,19 +12,28 @@
 //   - 32-bit, word b * 32 + lane, for 2D bin counts up to 35 (157 KB): the
 //     fastest layout there (17.2 updates/clock/SM in the inner loop alone,
 //     against 12.3 for the 16-slot layout);
-//   - 16-bit, two bins per word: word (b >> 1) * 32 + lane, half b & 1, for
-//     36 to 50 bins. Choosing the half costs instructions on every update and
-//     the loop ran at 10.8 updates/clock/SM, below the 16-slot layout, so this
-//     variant is only used on request.
+//   - 16-bit, for 36 to 50 bins (160 KB): the two bins (2h, c) and
+//     (2h + 1, c) of a pair share word (h * Bc + c) * 32 + lane. The row
+//     DOF's bins are staged from a second matrix that the preprocessing
+//     kernel writes as row codes (b >> 1) | (b & 1) << 7, so the word index
+//     comes from the same byte-pair IMAD as in the 32-bit layout, and the
+//     value added comes from one byte permute that replicates the code's top
+//     bit: 0x00000001 for an even row bin, 0xFFFF0001 (= 1 - 65536) for an
+//     odd one. A word then holds lo = n_even + n_odd in its low half and
+//     -n_odd mod 65536 in its high half (no carry crosses the halves while
+//     n_even + n_odd <= 65,535), i.e. n_odd = -hi mod 65536, n_even = lo - n_odd.
+//     At 50 bins it runs at 11.8 updates/clock/SM (2,048-frame chunks: the
+//     counters leave no room for 4,096), against 12.1 for the 16-slot layout,
+//     so the library picks the 16-slot layout there and this one on request.
 //
-// A 16-bit counter holds 65,535. No 2D bin of a pair can hold more frames
-// than the smaller of its two DOFs' largest marginal bin counts (computed by
-// the preprocessing kernel), so a tile whose pairs all stay within 65,535 by
-// that bound runs without any check. Other tiles (long trajectories with
-// peaked distributions) stop every 32,768 frames: the consumer warps move
-// 32,768 out of every counter that reached it into a per-CTA overflow count
-// in global memory (rare, L2-resident), so no counter can pass 65,535 within
-// the next 32,768 frames; the epilogue adds those counts back.
+// n_even + n_odd of a word counts frames in one column bin, so it cannot pass
+// the column DOF's largest marginal bin count (computed by the preprocessing
+// kernel): a tile whose column DOFs all stay within 65,535 runs without any
+// check. Other tiles (long trajectories with peaked distributions) stop every
+// 32,768 frames: the consumer warps move both counts of every word whose low
+// half reached 32,768 into a per-CTA overflow area in global memory (rare,
+// L2-resident) and clear the word, so no low half can pass 65,535 within the
+// next 32,768 frames; the epilogue adds those counts back.
 //
 // Persistent grid (one CTA per SM, tiles strided by the grid size), with the
 // warp-specialised TMA/mbarrier pipeline of the 16-slot kernel: the producer
@@ -61,7 +70,7 @@ constexpr int kSmemMax = 232448;
 // 32-bit counters (one bin per word) where they fit, else 16-bit halves
 __host__ __device__ constexpr bool wide_counters(int bmax) { return bmax <= kBmax32; }
 __host__ __device__ constexpr int words_per_lane(int bmax) {
-    return wide_counters(bmax) ? bmax * bmax : (bmax * bmax + 1) / 2;
+    return wide_counters(bmax) ? bmax * bmax : (bmax + 1) / 2 * bmax;
 }
 __host__ __device__ constexpr size_t hist32_bytes(int bmax) {
     return ((size_t)words_per_lane(bmax) * 32 * 4 + 127) / 128 * 128;
@@ -73,6 +82,17 @@ size_t smem_bytes(int bmax, int fc, int nst) {
 // hist word += 1, result unused (ordering from the barriers' clobbers)
 __device__ __forceinline__ void red_add1_nc(uint32_t saddr) { asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(saddr)); }
 
+// Value added for frame k (0..3) of a 4-frame word of row codes: bytes
+// 0x01, 0x00 (from the constant 1) and twice the sign of code byte k, i.e.
+// 0x00000001 for an even row bin and 0xFFFF0001 for an odd one.
+template <int K>
+__device__ __forceinline__ uint32_t half_value(uint32_t codes4) {
+    uint32_t r;
+    constexpr uint32_t sel = ((8u | K) << 12) | ((8u | K) << 8) | 0x54u;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(codes4), "r"(1u), "n"(sel));
+    return r;
+}
+
 struct Hist32Args {
     SysDesc one;  // single-system launch (tile_sys == nullptr)
     const SysDesc *many;
@@ -82,10 +102,9 @@ struct Hist32Args {
     const unsigned long long *nfix;
     double fix;
     int *err;
-    uint32_t *ovf_all;  // per CTA: [2 * words_per_lane][32] overflow counts (units of 32,768)
+    uint32_t *ovf_all;  // per CTA: [2 * words_per_lane][32] overflow counts
     int fc, nst, bmax;
     uint32_t kw, kneg;  // 128 (bytes per counter word row) and -128 * 65536
-    uint32_t k64, kneg64, khalf;  // 64, -64, 65535 (16-bit layout)
 };
 
 // W32: 32-bit counters, word idx * 32 + lane, reduction value 1, no folding.
@@ -144,7 +163,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                 const int k = lane;
                 const int g = k < kRows ? (k < tile.nrow ? tile.row0 + k : -1)
                                     : ((k - kRows) < tile.ncol ? tile.col0 + (k - kRows) : -1);
-                src = g >= 0 ? d.bins + (int64_t)g * d.geo.ldb : nullptr;
+                // 16-bit layout: row DOFs from the row-code matrix
+                const int64_t m = (!W32 && k < kRows) ? (int64_t)d.geo.D : 0;
+                src = g >= 0 ? d.bins + (m + g) * d.geo.ldb : nullptr;
             }
             const uint32_t bytes = (uint32_t)__popc(__ballot_sync(0xffffffffu, src != nullptr)) * (uint32_t)fc;
             for (int chunk = 0; chunk < nchunks; chunk++, seq++) {
@@ -195,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
             const uint32_t Bc = valid ? (uint32_t)d.dof.b2[gc] : 0u;
             // every warp holds all 32 slots, so this vote is the same in all
             // consumer warps (it decides who takes the fold barriers)
-            const bool risky = valid && min(d.dof.m2[gr], d.dof.m2[gc]) > 65535;
+            const bool risky = valid && (W32 ? false : d.dof.m2[gc] > 65535);
             const bool folding = !W32 && __any_sync(0xffffffffu, risky) && nchunks > fold_every;
             int g0 = warp;
             bool dead = false;  // a timed-out warp keeps taking the fold barriers
@@ -240,21 +261,25 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                                         for (int q = 0; q < 4; q++) red_add1_nc(ad[4 * q + k]);
                                     }
                                 } else {
-                                    // two frames per IMAD (idx < 2500 never carries into the
-                                    // upper half); word idx >> 1 of this lane, half idx & 1.
-                                    // The half's value (1 or 65536) and the second frame's
-                                    // address are formed with IMADs (runtime multipliers), the
-                                    // first frame's address on the ALU, to balance the two pipes
+                                    // word index (code & 0x7f) * Bc + bc, two frames per IMAD
+                                    // as above; the value from the code's top bit
 #pragma unroll
                                     for (int q = 0; q < 4; q++) {
+                                        const uint32_t rs = rw[q] & 0x7f7f7f7fu;
 #pragma unroll
                                         for (int h = 0; h < 2; h++) {
                                             const uint32_t sel = h ? 0x4342u : 0x4140u;
-                                            const uint32_t v = __byte_perm(rw[q], 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
+                                            const uint32_t v = __byte_perm(rs, 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
                                             const uint32_t hi = v >> 16;
-                                            const uint32_t b0 = v & 1u, b1 = hi & 1u;
-                                            red_add_nc(hbase + ((v & 0xfffeu) << 6), b0 * a.khalf + 1u);
-                                            red_add_nc(hi * a.k64 + hbase + b1 * a.kneg64, b1 * a.khalf + 1u);
+                                            const uint32_t a_hi = hi * a.kw + hbase;
+                                            const uint32_t a_lo = v * a.kw + hbase + hi * a.kneg;
+                                            if (h == 0) {
+                                                red_add_nc(a_lo, half_value<0>(rw[q]));
+                                                red_add_nc(a_hi, half_value<1>(rw[q]));
+                                            } else {
+                                                red_add_nc(a_lo, half_value<2>(rw[q]));
+                                                red_add_nc(a_hi, half_value<3>(rw[q]));
+                                            }
                                         }
                                     }
                                 }
@@ -265,9 +290,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                                     if (k < n) {
                                         const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
                                         const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                                        const uint32_t idx = br * Bc + bc;
-                                        if (W32) red_add1_nc(hbase + (idx << 7));
-                                        else red_add_nc(hbase + ((idx >> 1) << 7), (idx & 1u) * 0xffffu + 1u);
+                                        if (W32) red_add1_nc(hbase + ((br * Bc + bc) << 7));
+                                        else red_add_nc(hbase + (((br & 0x7fu) * Bc + bc) << 7),
+                                                       (br & 0x80u) ? 0xFFFF0001u : 1u);
                                     }
                                 }
                             }
@@ -279,17 +304,18 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                 g0 -= gstep;
                 if (g0 < 0) g0 += kConsumers;
                 if (folding && (chunk + 1) % fold_every == 0 && chunk + 1 < nchunks) {
-                    // every consumer's reductions so far are done; move
-                    // 32,768 out of each counter that reached it
+                    // every consumer's reductions so far are done; move both
+                    // counts of every word whose low half reached 32,768
+                    // out (w & 31 == lane: kConsumerThreads is a multiple of 32)
                     named_barrier(kConsumerThreads);
                     for (int w = ctid; w < nwords; w += kConsumerThreads) {
                         const uint32_t v = hist[w];
-                        if (v & 0x80008000u) {
-                            const uint32_t lo = (v >> 15) & 1u, hi = v >> 31;
-                            hist[w] = v - (lo << 15) - (hi << 31);
+                        if (v & 0x8000u) {
+                            const uint32_t n_odd = (0u - (v >> 16)) & 0xffffu, n_even = (v & 0xffffu) - n_odd;
+                            hist[w] = 0u;
                             const int b = (w >> 5) * 2;
-                            if (lo) ovf[b * 32 + lane] += 1u;
-                            if (hi) ovf[(b + 1) * 32 + lane] += 1u;
+                            ovf[b * 32 + lane] += n_even;
+                            ovf[(b + 1) * 32 + lane] += n_odd;
                             s_heavy[lane] = 1;
                         }
                     }
@@ -319,8 +345,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                 atomicAdd(&s_snl[lane], snl);
                 atomicAdd(&s_occ[lane], (unsigned int)occ);
             } else if (valid) {
-                const int nbin = d.dof.b2[egr] * d.dof.b2[egc];
-                const int nw = (nbin + 1) / 2;
+                // word j = h * Bc + c holds bins (2h, c) and (2h + 1, c)
+                const int Br = d.dof.b2[egr], Bcc = d.dof.b2[egc];
+                const int nw = (Br + 1) / 2 * Bcc;
                 const bool heavy = s_heavy[lane] != 0;
                 int64_t *dump = d.out.counts ? d.out.counts + (t * 32 + lane) * d.out.counts_bmax * d.out.counts_bmax
                                              : nullptr;
@@ -328,13 +355,14 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                     const int w = j * 32 + lane;
                     const uint32_t v = hist[w];
                     hist[w] = 0u;
-                    uint32_t n0 = v & 0xffffu, n1 = v >> 16;
+                    uint32_t n1 = (0u - (v >> 16)) & 0xffffu;  // odd row bin
+                    uint32_t n0 = (v & 0xffffu) - n1;           // even row bin
                     if (heavy) {
                         uint32_t *o = ovf + (size_t)(2 * j) * 32 + lane;
                         const uint32_t o0 = o[0], o1 = o[32];
                         if (o0 | o1) {
-                            n0 += o0 << 15;
-                            n1 += o1 << 15;
+                            n0 += o0;
+                            n1 += o1;
                             o[0] = 0u;
                             o[32] = 0u;
                         }
@@ -342,8 +370,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                     snl += __ldg(a.nfix + n0) + __ldg(a.nfix + n1);
                     occ += (n0 != 0u) + (n1 != 0u);
                     if (dump) {
-                        dump[2 * j] = n0;
-                        if (2 * j + 1 < nbin) dump[2 * j + 1] = n1;
+                        const int h = j / Bcc, c = j - h * Bcc;
+                        dump[2 * h * Bcc + c] = n0;
+                        if (2 * h + 1 < Br) dump[(2 * h + 1) * Bcc + c] = n1;
                     }
                 }
                 atomicAdd(&s_snl[lane], snl);
@@ -417,8 +446,11 @@ bool config(int bmax, int *fc, int *nst) {
     return false;
 }
 
-cudaError_t launch(Hist32Args &a, void *scratch, size_t scratch_bytes, cudaStream_t st) {
+// codes: the row-code matrix follows every system's bin matrix (required by
+// the 16-bit layout)
+cudaError_t launch(Hist32Args &a, bool codes, void *scratch, size_t scratch_bytes, cudaStream_t st) {
     if (!config(a.bmax, &a.fc, &a.nst)) return cudaErrorInvalidValue;
+    if (!wide_counters(a.bmax) && !codes) return cudaErrorInvalidValue;
     if (a.n_tiles <= 0) return cudaSuccess;
     const int grid = (int)std::min<int64_t>(a.n_tiles, sm_count());
     const size_t need = pairs_hist32_scratch_bytes(a.bmax, grid);
@@ -428,20 +460,14 @@ cudaError_t launch(Hist32Args &a, void *scratch, size_t scratch_bytes, cudaStrea
     a.ovf_all = (uint32_t *)scratch;
     a.kw = 128u;
     a.kneg = 0u - (128u << 16);
-    a.k64 = 64u;
-    a.kneg64 = 0u - 64u;
-    a.khalf = 0xffffu;
     const size_t smem = smem_bytes(a.bmax, a.fc, a.nst);
-    if (wide_counters(a.bmax)) {
-        e = cudaFuncSetAttribute(pairs_hist32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        pairs_hist32_kernel<true><<<grid, kThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(pairs_hist32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        pairs_hist32_kernel<false><<<grid, kThreads, smem, st>>>(a);
-    }
-    return cudaGetLastError();
+    auto go = [&](auto kern) -> cudaError_t {
+        cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e2 != cudaSuccess) return e2;
+        kern<<<grid, kThreads, smem, st>>>(a);
+        return cudaGetLastError();
+    };
+    return wide_counters(a.bmax) ? go(pairs_hist32_kernel<true>) : go(pairs_hist32_kernel<false>);
 }
 
 }  // namespace
@@ -497,12 +523,12 @@ cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const Dof
     a.fix = fix;
     a.err = err;
     a.bmax = bmax;
-    return launch(a, scratch, scratch_bytes, st);
+    return launch(a, g.codes != 0, scratch, scratch_bytes, st);
 }
 
-cudaError_t launch_pairs_hist32_batch(int bmax, const SysDesc *sys, const PairTile *tiles, const int *tile_sys,
-                                      int64_t n_tiles, const unsigned long long *nfix, double fix, int *err,
-                                      void *scratch, size_t scratch_bytes, cudaStream_t st) {
+cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, const PairTile *tiles,
+                                      const int *tile_sys, int64_t n_tiles, const unsigned long long *nfix,
+                                      double fix, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st) {
     if (!pairs_hist32_supported(bmax)) return cudaErrorInvalidValue;
     Hist32Args a{};
     a.many = sys;
@@ -513,7 +539,7 @@ cudaError_t launch_pairs_hist32_batch(int bmax, const SysDesc *sys, const PairTi
     a.fix = fix;
     a.err = err;
     a.bmax = bmax;
-    return launch(a, scratch, scratch_bytes, st);
+    return launch(a, codes, scratch, scratch_bytes, st);
 }
 
 }  // namespace pg

@@ -276,6 +276,8 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const double bs1 = __ddiv_rn(__dsub_rn(mx, mn), (double)B1);
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
     uint8_t *brow = bins + (int64_t)g * geo.ldb;
+    // row codes for the 16-bit 32-slot histogram layout: (b >> 1) | (b & 1) << 7
+    uint8_t *crow = geo.codes ? bins + ((int64_t)geo.D + g) * geo.ldb : nullptr;
     int bad = 0;
     {
         // d = fl64(x' - mn) (x' the shifted value for dihedrals) is formed in
@@ -318,6 +320,7 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
             brow[f] = (uint8_t)i2;
+            if (crow) crow[f] = (uint8_t)((i2 >> 1) | ((i2 & 1) << 7));
         }
     }
     if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);

@@ -53,6 +53,19 @@ def test_batch_matches_oracle(eng, bins):
     _check_against_oracle(trajs, bodies, trees, bins)
 
 
+@pytest.mark.parametrize("slots", ["16", "32"])
+def test_batch_both_histogram_layouts_at_50_bins(eng, monkeypatch, slots):
+    """At 50 bins the batch runs the 16-slot layout or, forced, the 32-slot
+    layout with 16-bit counters (row codes written per system)."""
+    monkeypatch.setenv("PG_HIST_SLOTS", slots)
+    bins = (50, 50, 50, 50, 47, 39)
+    # not the one-frame system: its MI values are rounding noise around 0,
+    # so its tree order is not defined by the data
+    trajs = _systems([s for s in SYSTEMS if s[1] > 1], seed0=21)
+    bodies, trees = eng.entropy_batch(trajs, bins)
+    _check_against_oracle(trajs, bodies, trees, bins)
+
+
 def test_batch_equals_single_calls_bitwise(eng):
     bins = (50,) * 6
     trajs = _systems(SYSTEMS, seed0=5)

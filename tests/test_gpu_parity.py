@@ -333,10 +333,12 @@ def test_large_properties(eng):
 
 
 @pytest.mark.parametrize("n_atoms,F,bins", [(40, 70000, (50,) * 6), (20, 3000, (10, 20, 30, 50, 20, 8)),
-                                            (30, 20000, (30,) * 6), (25, 5000, (20, 30, 35, 35, 20, 8))])
+                                            (30, 20000, (30,) * 6), (25, 5000, (20, 30, 35, 35, 20, 8)),
+                                            (22, 4001, (50, 50, 50, 37, 49, 41)), (14, 999, (5, 5, 5, 36, 1, 3))])
 def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
     """The 32-slot histogram layout (32-bit counters up to 35 bins, 16-bit
-    halves above) gives the same counts and values."""
+    counters for row-bin pairs above, odd row-bin counts included) gives the
+    same counts and values."""
     monkeypatch.setenv("PG_HIST_SLOTS", "32")
     t = _synth_case(n_atoms, F, 0, seed=n_atoms + F, frac_bimodal_dih=0.2)
     body = eng.entropy(t, bins, "hist")
