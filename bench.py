@@ -110,6 +110,9 @@ def parse():
                     help="atoms of the bounded DOF sample timed on the host cores "
                          "(0: sized to ~2.5e10 pair-frame updates, about 10 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batconv", action="store_true",
+                    help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
+                         "with the workload's atoms and frames (host coordinates in, device columns out)")
     ap.add_argument("--ingest", action="store_true",
                     help="instead of the step: write the workload as a .bat (under $TMPDIR) and time "
                          "pg_bat_read (host columns) against pg_bat_read_device (device columns)")
@@ -635,10 +638,58 @@ def run_ingest(args):
     return 0
 
 
+def run_batconv(args):
+    """Cartesian -> BAT throughput (pg_bat_from_cartesian): a jittering random
+    chain of the workload's atoms and frames in pinned host memory, FP64 and
+    FP32 columns out. Prints one JSON line."""
+    import ctypes as C
+
+    import numpy as np
+
+    import parent_gb300 as pg
+    n_atoms, F = WORKLOADS[args.workload][:2]
+    nd = n_atoms - 3
+    rng = np.random.default_rng(7)
+    steps = rng.normal(size=(n_atoms, 3)).astype(np.float32)
+    steps /= np.linalg.norm(steps, axis=1, keepdims=True)
+    base = np.cumsum(0.15 * steps, axis=0, dtype=np.float32)
+    xyz = np.empty((F, n_atoms, 3), np.float32)
+    jit = (0.01 * rng.normal(size=(4096, n_atoms, 3))).astype(np.float32)
+    for f0 in range(0, F, 4096):
+        n = min(4096, F - f0)
+        xyz[f0:f0 + n] = base[None] + jit[:n]
+    dih = np.zeros((nd, 6), np.int32)
+    for i in range(nd):
+        dih[i] = [i + 1, i + 2, i + 3, i + 4, 0, i if i % 3 == 1 else -1]
+    eng = pg.Engine(0)
+    res = {}
+    for prec in (1, 0):
+        times, dev = [], []
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            eng.bat_from_cartesian(xyz, dih, double_prec=prec)
+            dt = time.perf_counter() - t0
+            ms = (C.c_double * 5)()
+            pg.lib().pg_last_timings(eng.handle, ms)
+            if k >= args.warmup:
+                times.append(dt)
+                dev.append(ms[4] / 1e3)
+        s = statistics.median(times)
+        res["fp64" if prec else "fp32"] = {"s": round(s, 4), "device_s": round(statistics.median(dev), 4),
+                                           "frames_per_s": round(F / s), "dof_values_per_s": (3 * nd + 3) * F / s}
+    eng.close()
+    print(json.dumps({"metric": "Cartesian -> BAT conversion (xyz in host memory -> device BAT columns)",
+                      "input_bytes": int(xyz.nbytes), "results": res,
+                      "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.ingest:
         return run_ingest(args)
+    if args.batconv:
+        return run_batconv(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -201,6 +201,21 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
  * the dihedral shift modFit (PARENT.cpp:609; 0 for bonds/angles). */
 PG_API int pg_dof_stats(pg_ctx *ctx, double *mn, double *mx, double *shift);
 
+/* Cartesian -> BAT on the device, as BAT_builder converts an .xtc frame by
+ * frame (BAT_trajectory.cpp:114-125: coordinates x10 into Angstrom,
+ * convert_to_BAT :219-300, phase angles :303-310, shift into [0, 2 pi)
+ * :209-214). xyz: n_frames x (n_dihedrals + 3) x 3 floats in nm, frame-major
+ * as read_xtc returns them (host memory, or device memory when
+ * xyz_on_device = 1); dih: n_dihedrals x 6 ints as in the .bat header
+ * (atoms 1-based, [4] the type, [5] the parent dihedral 1-based or -1).
+ * *out receives a device view of the BAT columns (FP64 for double_prec = 1,
+ * else FP32, the values a .bat of that precision holds), owned by the
+ * context and valid until the next conversion or pg_destroy; pass it to
+ * pg_entropy. Bonds are bit-identical to BAT_builder's; angles and dihedrals
+ * use CUDA's acos/atan2 and can differ in the last place. */
+PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_device, int n_frames, int n_dihedrals,
+                                 const int *dih, int double_prec, pg_bat_view *out);
+
 /* ------------------------------------------------------------ file formats */
 
 /* Opaque .bat contents: header (atoms, dihedral table, masses) and DOF-major

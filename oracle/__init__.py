@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
         L.or_mutual.argtypes = [i, i, i, i] + [dp] * 9
         L.or_mie_totals.argtypes = [i] + [dp] * 9 + [dp]
         L.or_mist.argtypes = [i] + [dp] * 9 + [ip, ip, ip, ip, dp, ip, dp]
+        L.or_bat_from_xyz.argtypes = [i, i, C.POINTER(C.c_float), ip, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -162,3 +163,19 @@ def fmt12(x: float) -> str:
 
 def ref_available() -> bool:
     return (REF / "PARENT.x").exists()
+
+
+def bat_from_xyz(xyz: np.ndarray, dih: np.ndarray):
+    """Cartesian (F, nDih+3, 3) float32 in nm + the .bat dihedral table
+    (nDih, 6) -> FP64 columns (bonds, angles, dihedrals), as BAT_builder."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    dih = np.ascontiguousarray(dih, dtype=np.int32)
+    nf, na, _ = xyz.shape
+    nd = dih.shape[0]
+    assert na == nd + 3
+    b = np.empty((nd + 2, nf)); a = np.empty((nd + 1, nf)); d = np.empty((nd, nf))
+    rc = lib().or_bat_from_xyz(nd, nf, xyz.ctypes.data_as(C.POINTER(C.c_float)),
+                               dih.ctypes.data_as(C.POINTER(C.c_int)), _p(b), _p(a), _p(d))
+    if rc:
+        raise ValueError(f"or_bat_from_xyz: bad dihedral table ({rc})")
+    return b, a, d

@@ -528,3 +528,79 @@ void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const doub
     for (int t = 0; t < 3; t++) { free(In[t]); free(Out[t]); }
     for (int q = 0; q < 6; q++) free(M[q]);
 }
+
+/* ------------------------------------------------------- BAT conversion */
+
+/* One frame of BAT_Trajectory::convert_to_BAT (BAT_trajectory.cpp:219-300):
+ * difference vectors in float (the coordinates are float), everything after
+ * in double, in the reference's operation order. */
+static void or_bat_frame(int nd, const float *x, const int *dih, double *rb0, double *rb1, double *ra,
+                         double *bond, double *angle, double *dihe) {
+    double b1[3], b2[3], b3[3], A[3], B[3];
+    const int r0 = dih[0] - 1, r1 = dih[1] - 1, r2 = dih[2] - 1;
+    for (int c = 0; c < 3; c++) {
+        b2[c] = (double)(float)(x[3 * r1 + c] - x[3 * r0 + c]);  /* :235-237 */
+        b3[c] = (double)(float)(x[3 * r2 + c] - x[3 * r1 + c]);  /* :239-241 */
+    }
+    *rb0 = sqrt(b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2]);  /* :246 */
+    *rb1 = sqrt(b3[0] * b3[0] + b3[1] * b3[1] + b3[2] * b3[2]);  /* :247 */
+    *ra = acos((b2[0] * b3[0] + b2[1] * b3[1] + b2[2] * b3[2]) / *rb0 / *rb1);  /* :265 */
+    for (int i = 0; i < nd; i++) {  /* :270-298 */
+        const int *d = dih + 6 * i;
+        const int a0 = d[0] - 1, a1 = d[1] - 1, a2 = d[2] - 1, a3 = d[3] - 1;
+        for (int c = 0; c < 3; c++) {
+            b1[c] = (double)(float)(x[3 * a1 + c] - x[3 * a0 + c]);
+            b2[c] = (double)(float)(x[3 * a2 + c] - x[3 * a1 + c]);
+            b3[c] = (double)(float)(x[3 * a3 + c] - x[3 * a2 + c]);
+        }
+        const double bl = sqrt(b3[0] * b3[0] + b3[1] * b3[1] + b3[2] * b3[2]);
+        const double prev = sqrt(b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2]);
+        bond[i] = bl;
+        angle[i] = acos((b2[0] * b3[0] + b2[1] * b3[1] + b2[2] * b3[2]) / bl / prev);
+        A[0] = b1[1] * b2[2] - b1[2] * b2[1];
+        A[1] = b1[2] * b2[0] - b1[0] * b2[2];
+        A[2] = b1[0] * b2[1] - b1[1] * b2[0];
+        B[0] = b2[1] * b3[2] - b2[2] * b3[1];
+        B[1] = b2[2] * b3[0] - b2[0] * b3[2];
+        B[2] = b2[0] * b3[1] - b2[1] * b3[0];
+        dihe[i] = atan2((A[2] * B[0] - A[0] * B[2]) * b2[1] / prev - (A[2] * B[1] - A[1] * B[2]) * b2[0] / prev -
+                            (A[1] * B[0] - A[0] * B[1]) * b2[2] / prev,
+                        A[0] * B[0] + A[1] * B[1] + A[2] * B[2]);
+    }
+}
+
+int or_bat_from_xyz(int nd, int nf, const float *xyz, const int *dih, double *bonds, double *angles,
+                    double *dihedrals) {
+    const int na = nd + 3;
+    if (nd < 1 || nf < 1) return 1;
+    for (int i = 0; i < nd; i++) {
+        for (int k = 0; k < 4; k++)
+            if (dih[6 * i + k] < 1 || dih[6 * i + k] > na) return 2;
+        if (dih[6 * i + 5] != -1 && (dih[6 * i + 5] < 1 || dih[6 * i + 5] > nd)) return 3;
+    }
+    const double pi = acos(-1);  /* :51 */
+    float *x = (float *)malloc(sizeof(float) * 3 * (size_t)na);
+    double *bl = (double *)malloc(sizeof(double) * (size_t)nd * 3);
+    double *an = bl + nd, *dh = bl + 2 * (size_t)nd;
+    const size_t F = (size_t)nf;
+    for (size_t f = 0; f < F; f++) {
+        for (int j = 0; j < 3 * na; j++) x[j] = (float)(xyz[f * 3 * na + j] * 10.0);  /* :115-119 */
+        double rb0, rb1, ra;
+        or_bat_frame(nd, x, dih, &rb0, &rb1, &ra, bl, an, dh);
+        for (int i = 0; i < nd; i++)  /* :303-310, in place */
+            if (dih[6 * i + 5] != -1) dh[i] -= dh[dih[6 * i + 5] - 1];
+        for (int i = 0; i < nd; i++)  /* :209-214 */
+            dh[i] = dh[i] + 2 * pi - (double)((int)((dh[i] + 2 * pi) / (2 * pi)) * 2) * pi;
+        bonds[0 * F + f] = rb0;  /* :121-123 */
+        bonds[1 * F + f] = rb1;
+        angles[0 * F + f] = ra;
+        for (int i = 0; i < nd; i++) {
+            bonds[(2 + (size_t)i) * F + f] = bl[i];
+            angles[(1 + (size_t)i) * F + f] = an[i];
+            dihedrals[(size_t)i * F + f] = dh[i];
+        }
+    }
+    free(x);
+    free(bl);
+    return 0;
+}

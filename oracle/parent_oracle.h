@@ -81,6 +81,18 @@ void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const doub
              int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
              int *edge_left, double totals[10]);
 
+/* Cartesian -> BAT columns as BAT_builder converts a trajectory frame by
+ * frame (BAT_trajectory.cpp:114-125): coordinates scaled by 10 (nm ->
+ * Angstrom, stored back as float), convert_to_BAT (:219-300),
+ * convert_dihedrals_to_phaseangles (:303-310, in place, in dihedral order)
+ * and shift_dihedrals_0_2pi_range (:209-214). xyz: n_frames x (nDih+3) x 3
+ * floats; dih: nDih x 6 ints as in the .bat header (atoms 1-based, [5] the
+ * parent dihedral 1-based or -1). Output columns DOF-major as or_read_bat:
+ * bonds (nDih+2)*F, angles (nDih+1)*F, dihedrals nDih*F. Returns 0, or
+ * nonzero for an atom or parent index out of range. */
+int or_bat_from_xyz(int n_dihedrals, int n_frames, const float *xyz, const int *dih,
+                    double *bonds, double *angles, double *dihedrals);
+
 #ifdef __cplusplus
 }
 #endif

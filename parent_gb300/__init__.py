@@ -93,6 +93,7 @@ def lib() -> C.CDLL:
         "pg_dof_stats": (i, [vp, dp, dp, dp]),
         "pg_bat_read": (i, [cp, C.POINTER(vp)]),
         "pg_bat_read_device": (i, [cp, i, C.POINTER(vp)]),
+        "pg_bat_from_cartesian": (i, [vp, vp, i, i, i, C.POINTER(C.c_int), i, C.POINTER(BatView)]),
         "pg_bat_free": (None, [vp]),
         "pg_bat_view_of": (i, [vp, C.POINTER(BatView)]),
         "pg_bat_n_dihedrals": (i, [vp]),
@@ -258,6 +259,22 @@ class Engine:
         body = out.c() if keep_result else None
         _check(lib().pg_entropy(self._ctx, C.byref(v), b, f, C.byref(body) if body else None), self._ctx)
         return out if keep_result else None
+
+    def bat_from_cartesian(self, xyz: np.ndarray, dih: np.ndarray, double_prec: int = 1) -> BatView:
+        """BAT_builder's conversion on the GPU: xyz (frames, nDih+3, 3) float32
+        in nm (host array), dih the .bat dihedral table (nDih, 6). Returns a
+        device view of the BAT columns (valid until the next conversion)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+        dih = np.ascontiguousarray(dih, dtype=np.int32)
+        if xyz.ndim != 3 or xyz.shape[2] != 3 or dih.ndim != 2 or dih.shape[1] != 6:
+            raise PGError(PG_ERR_ARG, "xyz must be (frames, atoms, 3) and dih (n_dih, 6)")
+        if xyz.shape[1] != dih.shape[0] + 3:
+            raise PGError(PG_ERR_ARG, "atoms must equal n_dih + 3")
+        v = BatView()
+        _check(lib().pg_bat_from_cartesian(self._ctx, xyz.ctypes.data, 0, xyz.shape[0], dih.shape[0],
+                                           dih.ctypes.data_as(C.POINTER(C.c_int)), int(double_prec), C.byref(v)),
+               self._ctx)
+        return v
 
     def mist(self, n_dih: int, body: ParBody | None = None):
         """MIST tree: (edges as a structured numpy array, totals[10])."""

@@ -120,6 +120,9 @@ struct pg_ctx {
     // host trajectories: uploads run on their own stream, one event per DOF group
     cudaStream_t copy = nullptr;
     cudaEvent_t gev[16] = {};
+    // Cartesian -> BAT: output columns (valid until the next conversion or
+    // pg_destroy), per-chunk staging, coordinate rows, FP64 dihedrals, table
+    DevBuf bc_out, bc_stage, bc_soa, bc_tmp, bc_tab;
 };
 
 static int fail(pg_ctx *c, int code, const char *fmt, ...) {
@@ -523,7 +526,8 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn, &ctx->nfix,
-                      &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr})
+                      &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr,
+                      &ctx->bc_out, &ctx->bc_stage, &ctx->bc_soa, &ctx->bc_tmp, &ctx->bc_tab})
         b->release();
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->batch.release();
@@ -539,6 +543,75 @@ PG_API void pg_destroy(pg_ctx *ctx) {
 }
 
 PG_API const char *pg_last_error(const pg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_global_err.c_str(); }
+
+PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_device, int n_frames, int n_dihedrals,
+                                 const int *dih, int double_prec, pg_bat_view *out) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    if (!xyz || !dih || !out) return fail(ctx, PG_ERR_ARG, "null argument");
+    if (n_dihedrals < 1 || n_frames < 1) return fail(ctx, PG_ERR_ARG, "n_dihedrals (%d) or n_frames (%d) < 1",
+                                                     n_dihedrals, n_frames);
+    if (double_prec != 0 && double_prec != 1) return fail(ctx, PG_ERR_ARG, "double_prec must be 0 or 1");
+    const int nd = n_dihedrals, na = nd + 3;  // BAT_trajectory.cpp:80-83: natoms == nDih + 3
+    std::vector<int4> atoms((size_t)nd);
+    std::vector<int> parent((size_t)nd);
+    for (int i = 0; i < nd; i++) {
+        const int *r = dih + 6 * (size_t)i;
+        for (int k = 0; k < 4; k++)
+            if (r[k] < 1 || r[k] > na) return fail(ctx, PG_ERR_ARG, "dihedral %d: atom %d outside 1..%d", i + 1, r[k], na);
+        if (r[5] != -1 && (r[5] < 1 || r[5] > nd))
+            return fail(ctx, PG_ERR_ARG, "dihedral %d: parent %d outside 1..%d", i + 1, r[5], nd);
+        atoms[i] = make_int4(r[0] - 1, r[1] - 1, r[2] - 1, r[3] - 1);
+        parent[i] = r[5] == -1 ? -1 : r[5] - 1;
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int64_t F = n_frames, ld = (F + 31) / 32 * 32;
+    const size_t es = double_prec ? 8 : 4;
+    const int64_t fc = std::min<int64_t>(F, 65536);  // frames per chunk
+    const int64_t lds = (fc + 31) / 32 * 32;
+    CK(ctx->bc_out.ensure((size_t)(3 * (int64_t)nd + 3) * ld * es));
+    CK(ctx->bc_soa.ensure((size_t)3 * na * lds * sizeof(float)));
+    if (!double_prec) CK(ctx->bc_tmp.ensure((size_t)nd * lds * sizeof(double)));
+    if (!xyz_on_device) CK(ctx->bc_stage.ensure((size_t)fc * na * 3 * sizeof(float)));
+    CK(ctx->bc_tab.ensure((size_t)nd * (sizeof(int4) + sizeof(int))));
+    int4 *d_atoms = (int4 *)ctx->bc_tab.p;
+    int *d_parent = (int *)(d_atoms + nd);
+    CK(cudaMemcpyAsync(d_atoms, atoms.data(), sizeof(int4) * nd, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_parent, parent.data(), sizeof(int) * nd, cudaMemcpyHostToDevice, st));
+    char *o = (char *)ctx->bc_out.p;
+    void *bonds = o, *angles = o + (size_t)(nd + 2) * ld * es, *dihs = o + (size_t)(2 * nd + 3) * ld * es;
+    CK(cudaEventRecord(ctx->ev[0], st));
+    for (int64_t f0 = 0; f0 < F; f0 += fc) {
+        const int n = (int)std::min<int64_t>(fc, F - f0);
+        const float *src = xyz + (size_t)f0 * na * 3;
+        if (!xyz_on_device) {
+            CK(cudaMemcpyAsync(ctx->bc_stage.p, src, (size_t)n * na * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+            src = (const float *)ctx->bc_stage.p;
+        }
+        CK(launch_cart_transpose(src, n, na, (float *)ctx->bc_soa.p, lds, st));
+        double *tmp = double_prec ? (double *)dihs + f0 : (double *)ctx->bc_tmp.p;
+        const int64_t ldt = double_prec ? ld : lds;
+        CK(launch_bat_convert((const float *)ctx->bc_soa.p, lds, n, nd, d_atoms, bonds, angles, ld, f0, double_prec,
+                              tmp, ldt, st));
+        CK(launch_bat_phase(tmp, ldt, n, nd, d_parent, dihs, ld, f0, double_prec, st));
+        ctx->launches += 3;
+    }
+    CK(cudaEventRecord(ctx->ev[1], st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    ctx->timings[4] = ms;
+    out->n_dihedrals = nd;
+    out->n_frames = n_frames;
+    out->double_prec = double_prec;
+    out->on_device = 1;
+    out->ld = ld;
+    out->bonds = bonds;
+    out->angles = angles;
+    out->dihedrals = dihs;
+    return PG_OK;
+}
 
 PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
                       pg_par_body *out) {

@@ -171,6 +171,16 @@ cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, 
                                       const int *tile_sys, int64_t n_tiles, const unsigned long long *nfix,
                                       double fix, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
 
+// Cartesian -> BAT conversion (pg_batconv.cu): coordinates of a chunk of
+// frames to one row per (atom, xyz) scaled by 10; bonds/angles/raw dihedrals;
+// phase angles and the [0, 2 pi) shift. Columns ld elements apart, frames f0..
+cudaError_t launch_cart_transpose(const float *aos, int nf, int n_atoms, float *soa, int64_t lds, cudaStream_t st);
+cudaError_t launch_bat_convert(const float *soa, int64_t lds, int nf, int nd, const int4 *atoms, void *bonds,
+                               void *angles, int64_t ld, int64_t f0, int prec, double *dtmp, int64_t ldt,
+                               cudaStream_t st);
+cudaError_t launch_bat_phase(double *dtmp, int64_t ldt, int nf, int nd, const int *parent, void *dih, int64_t ld,
+                             int64_t f0, int prec, cudaStream_t st);
+
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const double *nlogn, PairOut out, int *err, cudaStream_t st,

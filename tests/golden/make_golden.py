@@ -13,7 +13,12 @@ Steps:
 4. run the reference PARENT.x (50 bins), get_PAR_MIE.x, get_PAR_MIST.x (one
    OpenMP thread: the canonical tie order) and get_PAR_info.x on both;
 5. copy the reference's shipped golden tails (sample_output_MIE.txt,
-   sample_output_MIST.txt) for the full-system pin.
+   sample_output_MIST.txt) for the full-system pin;
+6. decode the test system's .xtc with the reference's xdrfile (oracle/_ref/
+   xtc_dump.x) and keep the Cartesian coordinates of the atoms the subset's
+   dihedrals use, renumbered in order of first use, with the subset's
+   dihedral table (ubq_sub_xyz.npz): BAT_builder's conversion of exactly these
+   coordinates is ubq_sub.bat.
 Text outputs are stored gzip-compressed.
 """
 from __future__ import annotations
@@ -85,12 +90,37 @@ def reference_outputs(ref: Path, bat: Path, stem: str, work: Path) -> None:
     gz(work / f"{stem}_info.txt", HERE / f"{stem}_ref_info.txt.gz")
 
 
+def ubq_sub_cartesian(ref: Path, xtc: Path, full_bat: Path, work: Path, k: int) -> None:
+    """Step 6: Cartesian input of the BAT conversion for the first k dihedrals."""
+    import numpy as np
+    raw_path = work / "ubq_xyz.raw"
+    run([ref / "xtc_dump.x", xtc, raw_path], stdout=subprocess.DEVNULL)
+    raw = raw_path.read_bytes()
+    na, nf = struct.unpack_from("<2i", raw, 0)
+    xyz = np.frombuffer(raw[8:], dtype=np.float32).reshape(nf, na, 3)
+    braw = full_bat.read_bytes()
+    _, _, nd, _ = struct.unpack_from("<4i", braw, 0)
+    off = 16 + (nd + 3) * 51
+    dih = np.frombuffer(braw[off: off + nd * 24], dtype=np.int32).reshape(nd, 6)[:k].copy()
+    atoms = []
+    for row in dih:
+        for a in row[:4]:
+            if int(a) not in atoms:
+                atoms.append(int(a))
+    assert len(atoms) == k + 3 and (dih[:, 5] <= k).all()
+    renum = {a: i + 1 for i, a in enumerate(atoms)}
+    for row in dih:
+        row[:4] = [renum[int(a)] for a in row[:4]]
+    sub = np.ascontiguousarray(xyz[:, [a - 1 for a in atoms], :])
+    np.savez_compressed(HERE / "ubq_sub_xyz.npz", xyz=sub, dih=dih)
+
+
 def main() -> None:
     ref_root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     run(["make", "-s", "-C", ROOT / "oracle", "ref", f"REF_ROOT={ref_root}", "-j4"])
     ref = ROOT / "oracle" / "_ref"
-    work = ROOT / "_work" / "golden"
-    work.mkdir(parents=True, exist_ok=True)
+    import tempfile
+    work = Path(tempfile.mkdtemp(prefix="pg_golden_"))
 
     ts = ref_root / "test_system"
     run([ref / "BAT_builder.x", "-t", ts / "UBQ_UBM2.top", "-x", ts / "UBQ_UBM2.xtc", "-o",
@@ -105,6 +135,8 @@ def main() -> None:
 
     for name in ("sample_output_MIE.txt", "sample_output_MIST.txt"):
         shutil.copy(ts / "sample_output" / name, HERE / f"ubq_full_{name}")
+    ubq_sub_cartesian(ref, ts / "UBQ_UBM2.xtc", work / "ubq.bat", work, K_SUB)
+    shutil.rmtree(work, ignore_errors=True)
     print("fixtures written to", HERE)
 
 
