@@ -113,6 +113,9 @@ def parse():
     ap.add_argument("--batconv", action="store_true",
                     help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
                          "with the workload's atoms and frames (host coordinates in, device columns out)")
+    ap.add_argument("--mie", action="store_true",
+                    help="instead of the step: time get_PAR_MIE's text for a .par body of the workload's size "
+                         "with the host writer and with the device writer (files under $TMPDIR)")
     ap.add_argument("--ingest", action="store_true",
                     help="instead of the step: write the workload as a .bat (under $TMPDIR) and time "
                          "pg_bat_read (host columns) against pg_bat_read_device (device columns)")
@@ -684,10 +687,63 @@ def run_batconv(args):
     return 0
 
 
+def run_mie(args):
+    """MIE text throughput: a seeded random .par body with the workload's DOF
+    count written by pg_write_mie_text (host threads) and by
+    pg_write_mie_text_device (pair lines on the GPU); the two files must be
+    identical. Prints one JSON line."""
+    import hashlib
+    import shutil
+
+    import numpy as np
+
+    import parent_gb300 as pg
+    n_atoms = WORKLOADS[args.workload][0]
+    nd = n_atoms - 3
+    rng = np.random.default_rng(11)
+    body = pg.ParBody.empty(nd)
+    for v in body.blocks.values():
+        v[:] = rng.normal(2.0, 1.5, v.size)
+    lines = sum(v.size for v in body.blocks.values()) + 16  # one line per body value, 16 totals
+    d = Path(tempfile.mkdtemp(prefix="pg_mie_"))
+    eng = pg.Engine(0)
+    res = {}
+    try:
+        for name in ("host", "device"):
+            times = []
+            for k in range(args.warmup + args.steps):
+                path = d / f"{name}.txt"
+                t0 = time.perf_counter()
+                if name == "host":
+                    pg.write_mie_text(path, body)
+                else:
+                    eng.write_mie_text(path, body)
+                dt = time.perf_counter() - t0
+                if k >= args.warmup:
+                    times.append(dt)
+            h = hashlib.sha1()
+            with open(d / f"{name}.txt", "rb") as f:
+                while chunk := f.read(1 << 24):
+                    h.update(chunk)
+            s = statistics.median(times)
+            res[name] = {"s": round(s, 3), "lines_per_s": round(lines / s), "sha1": h.hexdigest(),
+                         "bytes": (d / f"{name}.txt").stat().st_size}
+    finally:
+        eng.close()
+        shutil.rmtree(d, ignore_errors=True)
+    print(json.dumps({"metric": "MIE text (get_PAR_MIE.x output) written to a file", "lines": lines,
+                      "identical": res["host"]["sha1"] == res["device"]["sha1"], "host_writer": res["host"],
+                      "device_writer": res["device"], "host_threads": os.cpu_count(),
+                      "config": {"workload": args.workload, "dofs": 3 * nd + 3}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.ingest:
         return run_ingest(args)
+    if args.mie:
+        return run_mie(args)
     if args.batconv:
         return run_batconv(args)
     if args.impl == "reference":

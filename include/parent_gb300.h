@@ -259,6 +259,15 @@ PG_API int pg_par_bins(const pg_par *par, int bins[6]);
  * get_PAR_MIE.cpp:109-199 (MIE), get_PAR_MIST.cpp:667-765 (MIST),
  * get_PAR_info.cpp:64-79 (topology). path NULL -> stdout. */
 PG_API int pg_write_mie_text(const char *path, int n_dihedrals, const pg_par_body *body);
+/* The same text, byte for byte, with the ~n^2/2 pair lines formatted on the
+ * context's GPU (one thread per line, %.12g in exact 128-bit integer
+ * arithmetic) and streamed back in order; the 1D lines and the totals (summed
+ * in the reference's line order) stay on the host. */
+PG_API int pg_write_mie_text_device(pg_ctx *ctx, const char *path, int n_dihedrals, const pg_par_body *body);
+/* printf("%.12g") of v into out (>= 32 bytes, NUL-terminated) by the exact
+ * formatter the device text writer uses (the C library's where that
+ * formatter's range ends); returns the length. Exported for verification. */
+PG_API int pg_format_g12(double v, char *out);
 PG_API int pg_write_mist_text(const char *path, int n_dihedrals, const pg_mist_edge *edges,
                               const double totals[10]);
 PG_API int pg_write_info_text(const char *path, const pg_par *par);

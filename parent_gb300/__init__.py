@@ -106,6 +106,8 @@ def lib() -> C.CDLL:
         "pg_par_body_of": (i, [vp, C.POINTER(ParBodyC)]),
         "pg_par_bins": (i, [vp, C.POINTER(C.c_int)]),
         "pg_write_mie_text": (i, [cp, i, C.POINTER(ParBodyC)]),
+        "pg_write_mie_text_device": (i, [vp, cp, i, C.POINTER(ParBodyC)]),
+        "pg_format_g12": (i, [C.c_double, cp]),
         "pg_write_mist_text": (i, [cp, i, C.POINTER(MistEdge), dp]),
         "pg_write_info_text": (i, [cp, vp]),
         "pg_synth_host": (i, [C.POINTER(SynthSpec), vp, vp, vp, i64, i]),
@@ -275,6 +277,12 @@ class Engine:
                                            dih.ctypes.data_as(C.POINTER(C.c_int)), int(double_prec), C.byref(v)),
                self._ctx)
         return v
+
+    def write_mie_text(self, path: str | Path | None, body: ParBody) -> None:
+        """get_PAR_MIE.x's text with the pair lines formatted on this GPU."""
+        bc = body.c()
+        _check(lib().pg_write_mie_text_device(self._ctx, str(path).encode() if path else None, body.n_dih,
+                                              C.byref(bc)), self._ctx)
 
     def mist(self, n_dih: int, body: ParBody | None = None):
         """MIST tree: (edges as a structured numpy array, totals[10])."""

@@ -42,6 +42,7 @@ CU_SOURCES = {
     "pg_noalloc.cu": [],
     "pg_ingest.cu": [],
     "pg_batconv.cu": ["--fmad=false"],
+    "pg_mie.cu": [],
 }
 CPP_SOURCES = ["pg_io.cpp"]
 CLIS = ["PARENT_gb300", "get_PAR_MIST_gb300", "get_PAR_MIE_gb300", "get_PAR_info_gb300"]

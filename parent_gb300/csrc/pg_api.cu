@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -123,6 +124,8 @@ struct pg_ctx {
     // Cartesian -> BAT: output columns (valid until the next conversion or
     // pg_destroy), per-chunk staging, coordinate rows, FP64 dihedrals, table
     DevBuf bc_out, bc_stage, bc_soa, bc_tmp, bc_tab;
+    // MIE text: body, line slots and lengths, row offsets, text, host fallbacks
+    DevBuf mie_body, mie_slots, mie_lens, mie_rows, mie_text, mie_fb;
 };
 
 static int fail(pg_ctx *c, int code, const char *fmt, ...) {
@@ -527,7 +530,8 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn, &ctx->nfix,
                       &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr,
-                      &ctx->bc_out, &ctx->bc_stage, &ctx->bc_soa, &ctx->bc_tmp, &ctx->bc_tab})
+                      &ctx->bc_out, &ctx->bc_stage, &ctx->bc_soa, &ctx->bc_tmp, &ctx->bc_tab, &ctx->mie_body,
+                      &ctx->mie_slots, &ctx->mie_lens, &ctx->mie_rows, &ctx->mie_text, &ctx->mie_fb})
         b->release();
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->batch.release();
@@ -543,6 +547,158 @@ PG_API void pg_destroy(pg_ctx *ctx) {
 }
 
 PG_API const char *pg_last_error(const pg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_global_err.c_str(); }
+
+}  // extern "C"
+
+namespace pg {
+int mie_lines_device(pg_ctx *ctx, int nd, const pg_par_body *b, const std::function<bool(const char *, size_t)> &sink);
+}
+
+// The 2D lines of the MIE text (get_PAR_MIE.cpp:109-199) formatted on the
+// device, handed to `sink` in order in pieces of at most 64 MB. Lines with a
+// value outside the device formatter's exact range are formatted here.
+int pg::mie_lines_device(pg_ctx *ctx, int nd, const pg_par_body *b,
+                         const std::function<bool(const char *, size_t)> &sink) {
+    if (!ctx || !b || nd < 0) return fail(ctx, PG_ERR_ARG, "mie: bad arguments");
+    ctx->err.clear();
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int nb = nd + 2, na = nd + 1;
+    const ParLayout L = par_layout(nd);
+    const double *hb[9] = {b->s1_b, b->s1_a, b->s1_d, b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
+    const int64_t off[9] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd};
+    const int64_t len9[9] = {L.s1a - L.s1b, L.s1d - L.s1a, L.bb - L.s1d, L.ba - L.bb, L.bd - L.ba,
+                             L.aa - L.bd, L.ad - L.aa, L.dd - L.ad, L.total - L.dd};
+    CK(ctx->mie_body.ensure((size_t)L.total * sizeof(double) + 64));
+    double *db = (double *)ctx->mie_body.p;
+    for (int k = 0; k < 9; k++)
+        if (len9[k] > 0) CK(cudaMemcpyAsync(db + off[k], hb[k], (size_t)len9[k] * sizeof(double), cudaMemcpyHostToDevice, st));
+    MieArgs a{};
+    static const char *nm[6] = {"bond-bond ", "bond-angle ", "bond-dihedral ", "angle-angle ", "angle-dihedral ",
+                                "dihedral-dihedral "};
+    const int n1[6] = {nb, nb, nb, na, na, nd}, n2[6] = {nb, na, nd, na, nd, nd}, same[6] = {1, 0, 0, 1, 0, 1};
+    const int64_t boff[6] = {L.bb, L.ba, L.bd, L.aa, L.ad, L.dd};
+    const int64_t s1o[3] = {L.s1b, L.s1a, L.s1d};
+    const int rt[6] = {0, 0, 0, 1, 1, 2}, ct[6] = {0, 1, 2, 1, 2, 2};
+    int64_t lines = 0;
+    int rows = 0;
+    for (int q = 0; q < 6; q++) {
+        a.blk[q] = db + boff[q];
+        a.s1r[q] = db + s1o[rt[q]];
+        a.s1c[q] = db + s1o[ct[q]];
+        a.n1[q] = n1[q];
+        a.n2[q] = n2[q];
+        a.same[q] = same[q];
+        a.line0[q] = lines;
+        a.row0[q] = rows;
+        const int64_t nl = same[q] ? (int64_t)n1[q] * (n1[q] - 1) / 2 : (int64_t)n1[q] * n2[q];
+        if (nl > 0) rows += same[q] ? n1[q] - 1 : n1[q];
+        lines += nl;
+        a.name_len[q] = (int)strlen(nm[q]);
+        memcpy(a.name[q], nm[q], (size_t)a.name_len[q]);
+    }
+    a.row0[6] = rows;
+    a.rows = rows;
+    if (lines == 0) return PG_OK;
+    constexpr int kFbCap = 1 << 16;
+    CK(ctx->mie_slots.ensure((size_t)lines * kMieSlot));
+    CK(ctx->mie_lens.ensure((size_t)lines));
+    CK(ctx->mie_rows.ensure((size_t)(2 * (int64_t)rows + 1) * sizeof(long long)));
+    CK(ctx->mie_fb.ensure(sizeof(int64_t) * (kFbCap + 1)));
+    a.slots = (char *)ctx->mie_slots.p;
+    a.lens = (uint8_t *)ctx->mie_lens.p;
+    a.row_len = (long long *)ctx->mie_rows.p;
+    a.row_off = a.row_len + rows;
+    a.fb_count = (int *)ctx->mie_fb.p;
+    a.fb_list = (int64_t *)ctx->mie_fb.p + 1;
+    a.fb_cap = kFbCap;
+    CK(cudaMemsetAsync(a.fb_count, 0, sizeof(int), st));
+    CK(launch_mie_format(a, st));
+    ctx->launches++;
+    int nfb = 0;
+    CK(cudaMemcpyAsync(&nfb, a.fb_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (nfb > kFbCap) return fail(ctx, PG_ERR_UNSUPPORTED, "mie: %d values outside the device formatter's range", nfb);
+    if (nfb > 0) {  // the C library formats these lines; they go into their slots
+        std::vector<int64_t> fl((size_t)nfb);
+        CK(cudaMemcpy(fl.data(), a.fb_list, sizeof(int64_t) * nfb, cudaMemcpyDeviceToHost));
+        const double *hs1[3] = {b->s1_b, b->s1_a, b->s1_d};
+        const double *hblk[6] = {b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
+        for (int64_t Lg : fl) {
+            int q = 5;
+            while (q > 0 && Lg < a.line0[q]) q--;
+            const int64_t Lq = Lg - a.line0[q];
+            int i, j;
+            double s2;
+            if (same[q]) {  // row i starts at i (n-1) - i (i-1) / 2
+                const int64_t n = n1[q];
+                int lo = 0, hi = n1[q] - 2;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) / 2;
+                    if ((int64_t)mid * (n - 1) - (int64_t)mid * (mid - 1) / 2 <= Lq) lo = mid; else hi = mid - 1;
+                }
+                i = lo;
+                j = i + 1 + (int)(Lq - ((int64_t)i * (n - 1) - (int64_t)i * (i - 1) / 2));
+                s2 = hblk[q][n * (n - 1) / 2 - 1 - Lq];
+            } else {
+                i = (int)(Lq / n2[q]);
+                j = (int)(Lq % n2[q]);
+                s2 = hblk[q][Lq];
+            }
+            const double mu = hs1[rt[q]][i] + hs1[ct[q]][j] - s2;
+            char line[kMieSlot + 64];
+            const int k = snprintf(line, sizeof line, "%s%d  %d   %.12g   %.12g\n", nm[q], i + 1, j + 1, s2, mu);
+            if (k <= 0 || k > kMieSlot) return fail(ctx, PG_ERR_UNSUPPORTED, "mie: line too long");
+            const uint8_t lk = (uint8_t)k;
+            CK(cudaMemcpy(a.slots + Lg * kMieSlot, line, (size_t)k, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(a.lens + Lg, &lk, 1, cudaMemcpyHostToDevice));
+        }
+    }
+    CK(launch_mie_offsets(a, st));
+    long long total = 0;
+    CK(cudaMemcpyAsync(&total, a.row_off + rows, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(ctx->mie_text.ensure((size_t)total + 64));
+    a.text = (char *)ctx->mie_text.p;
+    CK(launch_mie_compact(a, st));
+    ctx->launches += 3;
+    // to the host in pieces, the next piece copied while the sink writes one
+    constexpr size_t kPiece = (size_t)64 << 20;
+    char *pin[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    int rc = PG_OK;
+    for (int k = 0; k < 2 && rc == PG_OK; k++) {
+        if (cudaHostAlloc(&pin[k], kPiece, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming) != cudaSuccess)
+            rc = fail(ctx, PG_ERR_NOMEM, "mie: pinned staging");
+    }
+    const size_t T = (size_t)total, np = (T + kPiece - 1) / kPiece;
+    for (size_t k = 0; k < np && rc == PG_OK; k++) {
+        const int s = (int)(k & 1);
+        if (k == 0) {
+            cudaMemcpyAsync(pin[0], a.text, std::min(kPiece, T), cudaMemcpyDeviceToHost, st);
+            cudaEventRecord(done[0], st);
+        }
+        if (k + 1 < np) {
+            const size_t o = (k + 1) * kPiece;
+            cudaMemcpyAsync(pin[s ^ 1], a.text + o, std::min(kPiece, T - o), cudaMemcpyDeviceToHost, st);
+            cudaEventRecord(done[s ^ 1], st);
+        }
+        if (cudaEventSynchronize(done[s]) != cudaSuccess) {
+            rc = fail(ctx, PG_ERR_CUDA, "mie: copy");
+            break;
+        }
+        if (!sink(pin[s], std::min(kPiece, T - k * kPiece))) rc = fail(ctx, PG_ERR_IO, "mie: write failed");
+    }
+    cudaStreamSynchronize(st);
+    for (int k = 0; k < 2; k++) {
+        if (pin[k]) cudaFreeHost(pin[k]);
+        if (done[k]) cudaEventDestroy(done[k]);
+    }
+    return rc;
+}
+
+extern "C" {
 
 PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_device, int n_frames, int n_dihedrals,
                                  const int *dih, int double_prec, pg_bat_view *out) {

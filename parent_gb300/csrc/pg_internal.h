@@ -181,6 +181,31 @@ cudaError_t launch_bat_convert(const float *soa, int64_t lds, int nf, int nd, co
 cudaError_t launch_bat_phase(double *dtmp, int64_t ldt, int nf, int nd, const int *parent, void *dih, int64_t ld,
                              int64_t f0, int prec, cudaStream_t st);
 
+// MIE text on the device (pg_mie.cu): the six pair blocks of the 2D lines,
+// rows of each block in order (row0[q] .. row0[q+1]), lines numbered from
+// line0[q]; every line first goes to a 96-byte slot, then the rows are packed.
+constexpr int kMieSlot = 96;
+struct MieArgs {
+    const double *blk[6];          // .par body block of the pair type
+    const double *s1r[6], *s1c[6]; // 1D entropies of the row / column DOF type
+    int n1[6], n2[6], same[6];
+    int64_t line0[6];
+    int row0[7];
+    int rows;
+    char name[6][20];              // "bond-bond " ... "dihedral-dihedral "
+    int name_len[6];
+    char *slots;
+    uint8_t *lens;
+    long long *row_len, *row_off;  // rows, rows + 1
+    char *text;
+    int *fb_count;                 // lines left to the host formatter
+    int64_t *fb_list;
+    int fb_cap;
+};
+cudaError_t launch_mie_format(const MieArgs &a, cudaStream_t st);
+cudaError_t launch_mie_offsets(const MieArgs &a, cudaStream_t st);   // row_len, row_off (total at [rows])
+cudaError_t launch_mie_compact(const MieArgs &a, cudaStream_t st);   // slots -> text
+
 // tcgen05 one-hot pair kernel (same outputs as the histogram kernel).
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const double *nlogn, PairOut out, int *err, cudaStream_t st,

@@ -20,11 +20,13 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "../../include/parent_gb300.h"
+#include "pg_fmt.h"
 
 namespace {
 
@@ -32,6 +34,7 @@ namespace {
 
 namespace pg {
 void set_global_error(const char *msg);
+int mie_lines_device(pg_ctx *ctx, int nd, const pg_par_body *b, const std::function<bool(const char *, size_t)> &sink);
 cudaError_t launch_bat_transpose(const uint8_t *raw, int nf, int64_t rec, int off0, int es, int n_dih,
                                  uint8_t *cols, int64_t ld, int64_t f0, cudaStream_t st);
 }
@@ -612,6 +615,70 @@ int close_out(const char *path, FILE *f) { return path ? (fclose(f) == 0 ? PG_OK
 
 extern "C" {
 
+// MIE text pieces shared by the host and the device writers: the 1D lines
+// with their totals, and the 2D block totals summed in the reference's line
+// order (one thread: the order fixes the FP64 rounding).
+static void mie_head(Out &o, int n_dih, const pg_par_body *b, double t1[3]) {
+    const int nb = n_dih + 2, na = n_dih + 1, nd = n_dih;
+    t1[0] = t1[1] = t1[2] = 0.0;
+    for (int k = 0; k < nb; k++) { o.s("bond ").i(k + 1).s("   ").d(b->s1_b[k]).s("\n"); t1[0] += b->s1_b[k]; }
+    for (int k = 0; k < na; k++) { o.s("angle ").i(k + 1).s("   ").d(b->s1_a[k]).s("\n"); t1[1] += b->s1_a[k]; }
+    for (int k = 0; k < nd; k++) { o.s("dihedral ").i(k + 1).s("   ").d(b->s1_d[k]).s("\n"); t1[2] += b->s1_d[k]; }
+}
+static void mie_block_totals(int n_dih, const pg_par_body *b, double e[6], double m[6]) {
+    const int nb = n_dih + 2, na = n_dih + 1, nd = n_dih;
+    const int n1[6] = {nb, nb, nb, na, na, nd}, n2[6] = {nb, na, nd, na, nd, nd};
+    const double *blk[6] = {b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
+    for (int q = 0; q < 6; q++) {
+        e[q] = m[q] = 0.0;
+        const bool same = q == 0 || q == 3 || q == 5;
+        int64_t counter = (int64_t)n1[q] * (n1[q] - 1) / 2 - 1;
+        const int rows = same ? n1[q] - 1 : n1[q];
+        for (int i = 0; i < rows; i++)
+            for (int j = same ? i + 1 : 0; j < n2[q]; j++) {
+                e[q] += same ? blk[q][counter--] : blk[q][(int64_t)i * n2[q] + j];
+                m[q] += mutual(q, i, j, n_dih, b);
+            }
+    }
+}
+static void mie_tail(Out &o, const double t1[3], const double e[6], const double m[6]) {
+    o.s("TOTAL 1D BONDS ENTROPY = ").d(t1[0]).s("\n");
+    o.s("TOTAL 1D ANGLES ENTROPY = ").d(t1[1]).s("\n");
+    o.s("TOTAL 1D DIHEDRALS ENTROPY = ").d(t1[2]).s("\n");
+    const char *tn[6] = {"BONDS-BONDS", "BONDS-ANGLES", "BONDS-DIHEDRALS", "ANGLES-ANGLES", "ANGLES-DIHEDRALS", "DIHEDRALS-DIHEDRALS"};
+    for (int q = 0; q < 6; q++) {
+        o.s("TOTAL 2D ").s(tn[q]).s(" ENTROPY = ").d(e[q]).s("\n");
+        o.s("TOTAL 2D ").s(tn[q]).s(" MUTUAL INFORMATION = ").d(m[q]).s("\n");
+    }
+    o.s("TOTAL CONFIGURATIONAL ENTROPY = ").d(t1[0] + t1[1] + t1[2] - m[0] - m[1] - m[2] - m[3] - m[4] - m[5]).s("\n");
+}
+
+PG_API int pg_write_mie_text_device(pg_ctx *ctx, const char *path, int n_dih, const pg_par_body *b) {
+    if (!ctx || !b || n_dih < 0) return ioerr(PG_ERR_ARG, "pg_write_mie_text_device: bad arguments");
+    FILE *f = open_out(path);
+    if (!f) return ioerr(PG_ERR_IO, "ERROR: COULD NOT OPEN FILE %s !", path);
+    int rc = PG_OK;
+    {
+        Out o(f);
+        double t1[3], e[6], m[6];
+        mie_head(o, n_dih, b, t1);
+        o.flush();
+        std::thread totals([&] { mie_block_totals(n_dih, b, e, m); });  // overlaps the device formatting
+        rc = pg::mie_lines_device(ctx, n_dih, b, [&](const char *p, size_t n) { return fwrite(p, 1, n, f) == n; });
+        totals.join();
+        if (rc == PG_OK) mie_tail(o, t1, e, m);
+    }
+    const int rc2 = close_out(path, f);
+    return rc != PG_OK ? rc : rc2;
+}
+
+PG_API int pg_format_g12(double v, char *out) {
+    const int n = pg::format_g12(v, out);
+    if (n < 0) return snprintf(out, 32, "%.12g", v);
+    out[n] = 0;
+    return n;
+}
+
 PG_API int pg_write_mie_text(const char *path, int n_dih, const pg_par_body *b) {
     if (!b || n_dih < 0) return ioerr(PG_ERR_ARG, "pg_write_mie_text: bad arguments");
     FILE *f = open_out(path);
@@ -619,10 +686,8 @@ PG_API int pg_write_mie_text(const char *path, int n_dih, const pg_par_body *b) 
     {
         Out o(f);
         const int nb = n_dih + 2, na = n_dih + 1, nd = n_dih;
-        double tB = 0, tA = 0, tD = 0, e[6] = {0}, m[6] = {0};
-        for (int k = 0; k < nb; k++) { o.s("bond ").i(k + 1).s("   ").d(b->s1_b[k]).s("\n"); tB += b->s1_b[k]; }
-        for (int k = 0; k < na; k++) { o.s("angle ").i(k + 1).s("   ").d(b->s1_a[k]).s("\n"); tA += b->s1_a[k]; }
-        for (int k = 0; k < nd; k++) { o.s("dihedral ").i(k + 1).s("   ").d(b->s1_d[k]).s("\n"); tD += b->s1_d[k]; }
+        double t1[3], e[6] = {0}, m[6] = {0};
+        mie_head(o, n_dih, b, t1);
         const char *nm[6] = {"bond-bond ", "bond-angle ", "bond-dihedral ", "angle-angle ", "angle-dihedral ", "dihedral-dihedral "};
         const int n1[6] = {nb, nb, nb, na, na, nd}, n2[6] = {nb, na, nd, na, nd, nd};
         const double *blk[6] = {b->bb, b->ba, b->bd, b->aa, b->ad, b->dd};
@@ -684,15 +749,7 @@ PG_API int pg_write_mie_text(const char *path, int n_dih, const pg_par_body *b) 
                 fwrite(sbuf.data(), 1, sbuf.size(), f);
             }
         }
-        o.s("TOTAL 1D BONDS ENTROPY = ").d(tB).s("\n");
-        o.s("TOTAL 1D ANGLES ENTROPY = ").d(tA).s("\n");
-        o.s("TOTAL 1D DIHEDRALS ENTROPY = ").d(tD).s("\n");
-        const char *tn[6] = {"BONDS-BONDS", "BONDS-ANGLES", "BONDS-DIHEDRALS", "ANGLES-ANGLES", "ANGLES-DIHEDRALS", "DIHEDRALS-DIHEDRALS"};
-        for (int q = 0; q < 6; q++) {
-            o.s("TOTAL 2D ").s(tn[q]).s(" ENTROPY = ").d(e[q]).s("\n");
-            o.s("TOTAL 2D ").s(tn[q]).s(" MUTUAL INFORMATION = ").d(m[q]).s("\n");
-        }
-        o.s("TOTAL CONFIGURATIONAL ENTROPY = ").d(tB + tA + tD - m[0] - m[1] - m[2] - m[3] - m[4] - m[5]).s("\n");
+        mie_tail(o, t1, e, m);
     }
     return close_out(path, f);
 }

@@ -142,10 +142,12 @@ def test_cli_usage_errors():
 
 
 def test_cli_host_formatters(tmp_path):
-    """get_PAR_MIE / get_PAR_info drop-ins need no GPU: byte-identical stdout."""
+    """get_PAR_MIE (host writer) / get_PAR_info drop-ins need no GPU:
+    byte-identical stdout."""
+    import os
     import subprocess
     r = subprocess.run([str(pg.BIN_DIR / "get_PAR_MIE_gb300"), str(GOLDEN / "ubq_sub_ref.par")],
-                       capture_output=True, text=True, check=True)
+                       capture_output=True, text=True, check=True, env=dict(os.environ, PG_MIE_WRITER="host"))
     assert r.stdout.splitlines() == read_text_gz("ubq_sub_ref_MIE.txt.gz")
     r = subprocess.run([str(pg.BIN_DIR / "get_PAR_info_gb300"), str(GOLDEN / "ubq_sub_ref.par")],
                        capture_output=True, text=True, check=True)
