@@ -181,6 +181,10 @@ cudaError_t launch_bat_convert(const float *soa, int64_t lds, int nf, int nd, co
 cudaError_t launch_bat_phase(double *dtmp, int64_t ldt, int nf, int nd, const int *parent, void *dih, int64_t ld,
                              int64_t f0, int prec, cudaStream_t st);
 
+// Host -> device copy by SM loads where the GPU can read the host memory
+// (pg_ingest.cu), else by the copy engine.
+cudaError_t h2d_copy(void *dst, const void *src, size_t bytes, cudaStream_t st, bool *pulled);
+
 // MIE text on the device (pg_mie.cu): the six pair blocks of the 2D lines,
 // rows of each block in order (row0[q] .. row0[q+1]), lines numbered from
 // line0[q]; every line first goes to a 96-byte slot, then the rows are packed.
