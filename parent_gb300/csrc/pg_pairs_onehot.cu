@@ -7,17 +7,22 @@
 // histogram of the pair, so the counts PARENT.cpp fills frame by frame
 // (e.g. :802-804) are entries of C.
 //
-// One CTA computes one 128 x 512 tile of C over all frames with
-// tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256, K=32, two accumulators
-// sharing the A tile): A and B are E4M3 one-hot tiles (2.0 = 0x40, 0.0 = 0x00)
-// built in shared memory from the uint8 bin rows, the accumulators are FP32
-// in tensor memory (all 512 columns) holding 4 x the count, exact below 2^24
-// (frames below 2^22). Warp-specialised: 15 builder warps load the tile's bin
-// rows two 128-frame K-blocks ahead (a 4-buffer ring) and expand each K-block
-// into a 2-stage ring of one-hot tiles, arriving on the stage's "full"
-// mbarrier; warp 15 waits on it, issues the block's eight MMAs and commits
-// them to the stage's "empty" mbarrier, which the builders wait on before
-// rebuilding the stage. No CTA-wide barrier inside the K loop.
+// A pair of CTAs (a cluster of 2, one per SM) computes one 256 x 512 tile of
+// C over all frames with tcgen05.mma.cta_group::2.kind::f8f6f4 (M=256, N=256,
+// K=32, two accumulators sharing the A tile): each CTA builds its 128 rows of
+// A and, of each 256-column MMA, 128 rows of B as E4M3 one-hot tiles (2.0 =
+// 0x40, 0.0 = 0x00) in its shared memory from the uint8 bin rows, and holds
+// its 128 rows x 512 columns of FP32 accumulators in tensor memory (4 x the
+// count, exact below 2^24: frames below 2^22). Against one CTA per 128 x 512
+// tile (still built as PAIR = false) each SM builds 384 instead of 640 rows
+// per K-block. Warp-specialised: 15 builder warps load the tile's bin rows
+// two 128-frame K-blocks ahead (a 4-buffer ring) and expand each K-block into
+// a ring of one-hot stages, arriving on the stage's "full" mbarrier; in the
+// pair's first CTA warp 15 waits on it, issues the block's eight MMAs and
+// commits them to the stage's "empty" mbarrier in both CTAs, which the
+// builders wait on before rebuilding the stage; in the second CTA warp 15
+// relays the stage's completion to the first. No CTA-wide barrier inside the
+// K loop.
 //
 // Epilogue: tcgen05.ld brings each row's counts to registers; every count n>0
 // of a pair (g1 < g2) adds round(2^s n ln n) (an int64 table) and 1 to the
@@ -45,23 +50,32 @@ constexpr int kLoaderWarp = 15;
 constexpr int kM = 128, kN = 512;      // tile of C: two 128 x 256 accumulators share one A tile
 constexpr int kNH = 256;               // N of one MMA
 constexpr int kKB = 128;               // frames per K-block (bytes per row per stage)
-constexpr int kStages = 2;
 constexpr int kAStage = kM * kKB;      // 16 KB
-constexpr int kBStage = kN * kKB;      // 64 KB
-constexpr int kStageBytes = kAStage + kBStage;
 constexpr int kMaxRowDofs = 18, kMaxColDofs = 66;  // 2D bins >= 8
 constexpr int kBinSlots = kMaxRowDofs + kMaxColDofs;
 constexpr int kBinBufBytes = kBinSlots * kKB;      // one K-block of the tile's bin rows
 constexpr int kBinBufs = 4;                        // ring of K-block bin rows, loaded two blocks ahead
-// byte offsets inside the dynamic shared memory
-constexpr int kOffBar = kStages * kStageBytes;     // full[kStages] | empty[kStages] | binfull[kBinBufs]
-constexpr int kNumBars = 2 * kStages + kBinBufs;
-constexpr int kOffTmem = kOffBar + kNumBars * 8;
-constexpr int kOffPsSnl = (kOffTmem + 16 + 15) / 16 * 16;
-constexpr int kOffPsOcc = kOffPsSnl + kMaxRowDofs * kMaxColDofs * 8;
-constexpr int kOffBins = (kOffPsOcc + kMaxRowDofs * kMaxColDofs * 4 + 127) / 128 * 128;
-constexpr int kSmemBytes = kOffBins + kBinBufs * kBinBufBytes;
-static_assert(kSmemBytes <= 227 * 1024, "one-hot kernel shared memory");
+
+// Shared-memory layout of one CTA. PAIR: a CTA pair computes a 256 x 512
+// tile with tcgen05.mma.cta_group::2 (M = 256); each CTA builds its 128 A
+// rows and half of the B rows (128 of each 256-column MMA), so a CTA's stage
+// holds 128 + 256 rows instead of 128 + 512.
+template <bool PAIR>
+struct OhCfg {
+    static constexpr int kBRows = PAIR ? 256 : 512;  // B rows built by this CTA
+    static constexpr int kStages = PAIR ? 3 : 2;
+    static constexpr int kBStage = kBRows * kKB;
+    static constexpr int kStageBytes = kAStage + kBStage;
+    // byte offsets inside the dynamic shared memory
+    static constexpr int kOffBar = kStages * kStageBytes;  // full[kStages] | empty[kStages] | binfull[kBinBufs]
+    static constexpr int kNumBars = 2 * kStages + kBinBufs;
+    static constexpr int kOffTmem = kOffBar + kNumBars * 8;
+    static constexpr int kOffPsSnl = (kOffTmem + 16 + 15) / 16 * 16;
+    static constexpr int kOffPsOcc = kOffPsSnl + kMaxRowDofs * kMaxColDofs * 8;
+    static constexpr int kOffBins = (kOffPsOcc + kMaxRowDofs * kMaxColDofs * 4 + 127) / 128 * 128;
+    static constexpr int kSmemBytes = kOffBins + kBinBufs * kBinBufBytes;
+    static_assert(kSmemBytes <= 227 * 1024, "one-hot kernel shared memory");
+};
 constexpr long long kWaitCycles = 4000000000LL;
 // Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
 
@@ -110,6 +124,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 // Instruction descriptor: D = F32, A = B = E4M3, both K-major, N = 256, M = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kNH >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
+constexpr uint32_t kIdesc2 = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kNH >> 3) << 17) |
+                             ((uint32_t)((2 * kM) >> 4) << 24);  // M = 256 over a CTA pair
 
 // E4M3 one-hot of 4 bins against a bin replicated in t4: 0x40 (2.0) in every
 // byte where w equals t4, 0x00 elsewhere (bins below 128). x = w ^ t4 has a
@@ -134,8 +150,59 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                  : "memory");
 }
-
-__device__ __forceinline__ unsigned char *bin_buffer(unsigned char *smem) { return smem + kOffBins; }
+// CTA pair: A and B halves from both CTAs' shared memory at the same offsets,
+// the accumulator rows of each CTA in its own tensor memory
+__device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc2), "r"(acc)
+        : "memory");
+}
+// completion of the pair's MMAs, signalled on the barrier at this offset in both CTAs
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+        "h"((unsigned short)3)
+        : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// shared::cluster address of the same variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+// arrive (release at cluster scope) on a barrier given by its cluster address
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t caddr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait_cluster(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 struct TcTile {
     int mt, nt;  // row tile (x128) and column tile (x512) of C
@@ -150,45 +217,70 @@ struct Item {
     int valid;
 };
 
+// One CTA (PAIR = false) computes the 128 x 512 tile (mt, nt) of C; a CTA
+// pair (PAIR, cluster of 2) the 256 x 512 tile (mt, nt), CTA `rank` owning
+// rows 256 mt + 128 rank .. +127 and, of each 256-column MMA, B columns
+// 128 rank .. +127. Only the pair's rank 0 issues MMAs. Builder warps arrive
+// on their own CTA's "full" barrier (CTA scope); in rank 1, warp 15 waits for
+// that and relays it with one cluster-scope arrival on rank 0's "full"
+// barrier (one cluster-scope release per stage instead of one per builder
+// warp, whose memory barriers stalled the builders). The commit of a stage's
+// MMAs arrives on the "empty" barrier of both CTAs.
+template <bool PAIR>
 __global__ void __launch_bounds__(kThreads, 1)
 onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
               const uint32_t *__restrict__ rowinfo,  // (dof << 8) | bin for each row of C
               const TcTile *__restrict__ tiles, const int64_t *__restrict__ nlogn_fix,
               unsigned long long *__restrict__ acc_snl, unsigned int *__restrict__ acc_occ, int D,
               int *err) {
+    using C = OhCfg<PAIR>;
+    constexpr int kStages = C::kStages, kStageBytes = C::kStageBytes, kBRows = C::kBRows;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *stages = smem;  // kStages x (A | B), 1024-B aligned
-    uint64_t *full = (uint64_t *)(smem + kOffBar);  // stage built (one arrival per builder warp)
-    uint64_t *empty = full + kStages;               // stage's MMAs done (tcgen05.commit)
-    uint64_t *binfull = empty + kStages;            // K-block bin rows stored (one arrival per builder warp)
-    uint32_t *tmem_slot = (uint32_t *)(smem + kOffTmem);
-    unsigned long long *ps_snl = (unsigned long long *)(smem + kOffPsSnl);  // [kMaxRowDofs][kMaxColDofs]
-    unsigned int *ps_occ = (unsigned int *)(smem + kOffPsOcc);
-    __shared__ int s_r0dof, s_c0dof;
+    uint64_t *full = (uint64_t *)(smem + C::kOffBar);  // stage built (one arrival per builder warp, both CTAs)
+    uint64_t *empty = full + kStages;                  // stage's MMAs done (tcgen05.commit)
+    uint64_t *binfull = empty + kStages;               // K-block bin rows stored (one arrival per builder warp)
+    uint32_t *tmem_slot = (uint32_t *)(smem + C::kOffTmem);
+    unsigned long long *ps_snl = (unsigned long long *)(smem + C::kOffPsSnl);  // [kMaxRowDofs][kMaxColDofs]
+    unsigned int *ps_occ = (unsigned int *)(smem + C::kOffPsOcc);
+    __shared__ int s_r0dof, s_c0dof, s_b0dof;
     __shared__ int s_cdof[kN];  // DOF of each column of the tile (-1 past R)
     __shared__ volatile int s_abort;
     __shared__ int s_mma_issued;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const TcTile tile = tiles[blockIdx.x];
-    const int r0 = tile.mt * kM, c0 = tile.nt * kN;
+    const uint32_t rank = PAIR ? cluster_rank() : 0u;
+    const TcTile tile = tiles[PAIR ? blockIdx.x >> 1 : blockIdx.x];
+    const int r0 = PAIR ? tile.mt * 2 * kM + (int)rank * kM : tile.mt * kM;  // this CTA's A rows
+    const int c0 = tile.nt * kN;
+    const int b0 = PAIR ? c0 + (int)rank * (kNH / 2) : c0;  // first C column of this CTA's B rows
 
     if (warp == 0) {  // all 512 TMEM columns: two 128 x 256 FP32 accumulators
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(512)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        if (PAIR) {
+            asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                             smem_u32(tmem_slot)),
+                         "r"(512)
+                         : "memory");
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+        } else {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                             smem_u32(tmem_slot)),
+                         "r"(512)
+                         : "memory");
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        }
     }
     for (int c = tid; c < kN; c += kThreads) s_cdof[c] = c0 + c < R ? (int)(rowinfo[c0 + c] >> 8) : -1;
     if (tid == 0) {
         for (int k = 0; k < kStages; k++) {
-            mbar_init(smem_u32(&full[k]), kBuilderWarps);
+            mbar_init(smem_u32(&full[k]), (PAIR && rank == 0) ? kBuilderWarps + 1 : kBuilderWarps);
             mbar_init(smem_u32(&empty[k]), 1);
         }
         for (int k = 0; k < kBinBufs; k++) mbar_init(smem_u32(&binfull[k]), kBuilderWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_r0dof = (int)(rowinfo[r0] >> 8);
+        s_r0dof = (int)(rowinfo[r0 < R ? r0 : R - 1] >> 8);
         s_c0dof = (int)(rowinfo[c0 < R ? c0 : R - 1] >> 8);
+        s_b0dof = (int)(rowinfo[b0 < R ? b0 : R - 1] >> 8);
         s_abort = 0;
         s_mma_issued = 0;
     }
@@ -197,51 +289,76 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
         ps_occ[i] = 0u;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    if (PAIR) cluster_sync_all();  // both CTAs' barriers exist before any remote arrival
+    else __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const int rdof0 = s_r0dof, cdof0 = s_c0dof;
+    const int rdof0 = s_r0dof, bdof0 = s_b0dof;
     const int rlast = (int)(rowinfo[min(r0 + kM, R) - 1] >> 8);
-    const int clast = (int)(rowinfo[min(c0 + kN, R) - 1] >> 8);
+    const int blast = (int)(rowinfo[min(b0 + (PAIR ? kN - kNH / 2 : kN), R) - 1] >> 8);  // last B row's DOF
     const int nkb = (F + kKB - 1) / kKB;
-    unsigned char *binbuf = bin_buffer(smem);  // [kBinBufs][kBinSlots][kKB]
+    unsigned char *binbuf = smem + C::kOffBins;  // [kBinBufs][kBinSlots][kKB]
 
     if (warp == kLoaderWarp) {
         // ------------------------------------------------------- MMA issuer
-        const uint32_t sbase = smem_u32(stages);
-        int kb = 0;
-        for (; kb < nkb; kb++) {
-            const int s = kb % kStages;
-            int ok = 1;
-            if (lane == 0) ok = mbar_wait_bounded(smem_u32(&full[s]), (uint32_t)((kb / kStages) & 1)) ? 1 : 0;
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (!ok || s_abort) {
-                if (lane == 0) s_abort = 1;
-                break;
-            }
-            if (lane == 0) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t a0 = sbase + s * kStageBytes, b0 = a0 + kAStage;
-#pragma unroll
-                for (int kk = 0; kk < kKB / 32; kk++) {
-#pragma unroll
-                    for (int h = 0; h < kN / kNH; h++) {  // B rows h*256.. start 32 row groups (32 KB) further
-                        mma_f8(tmem + h * kNH, smem_desc(a0 + kk * 256, 128, 1024),
-                               smem_desc(b0 + h * (kNH / 8) * 1024 + kk * 256, 128, 1024), (kb | kk) != 0);
-                    }
+        if (!PAIR || rank == 0) {
+            const uint32_t sbase = smem_u32(stages);
+            int kb = 0;
+            for (; kb < nkb; kb++) {
+                const int s = kb % kStages;
+                int ok = 1;
+                if (lane == 0)
+                    ok = (PAIR ? mbar_wait_cluster_bounded(smem_u32(&full[s]), (uint32_t)((kb / kStages) & 1))
+                               : mbar_wait_bounded(smem_u32(&full[s]), (uint32_t)((kb / kStages) & 1)))
+                             ? 1
+                             : 0;
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok || s_abort) {
+                    if (lane == 0) s_abort = 1;
+                    break;
                 }
-                mma_commit(smem_u32(&empty[s]));
+                if (lane == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a0 = sbase + s * kStageBytes, bb0 = a0 + kAStage;
+#pragma unroll
+                    for (int kk = 0; kk < kKB / 32; kk++) {
+#pragma unroll
+                        for (int h = 0; h < kN / kNH; h++) {  // B rows of MMA h start kBRows/2 rows further
+                            const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
+                            const uint64_t bd = smem_desc(bb0 + h * (kBRows / 2 / 8) * 1024 + kk * 256, 128, 1024);
+                            if (PAIR) mma_f8_pair(tmem + h * kNH, ad, bd, (kb | kk) != 0);
+                            else mma_f8(tmem + h * kNH, ad, bd, (kb | kk) != 0);
+                        }
+                    }
+                    if (PAIR) mma_commit_pair(smem_u32(&empty[s]));
+                    else mma_commit(smem_u32(&empty[s]));
+                }
+                __syncwarp();
             }
-            __syncwarp();
+            if (lane == 0) s_mma_issued = kb;
+        } else if (PAIR) {
+            // ------------------------------------------ rank 1: stage relay
+            const uint32_t full_c0 = map_to_rank(smem_u32(&full[0]), 0u);
+            for (int kb = 0; kb < nkb; kb++) {
+                const int s = kb % kStages;
+                int ok = 1;
+                if (lane == 0) ok = mbar_wait_bounded(smem_u32(&full[s]), (uint32_t)((kb / kStages) & 1)) ? 1 : 0;
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (!ok || s_abort) {
+                    if (lane == 0) s_abort = 1;
+                    break;
+                }
+                if (lane == 0) mbar_arrive_cluster(full_c0 + (uint32_t)s * 8u);
+                __syncwarp();
+            }
         }
-        if (lane == 0) s_mma_issued = kb;
     } else {
         // ----------------------------------------------------------- builders
-        // items: A rows 0..127 (1024 items), then B rows 0..511 (4096 items);
-        // item i -> (row group g, chunk c, row-in-group rr) with rr fastest, so
-        // 8 consecutive threads store one contiguous 128-B core matrix
-        constexpr int kItems = (kM + kN) * (kKB / 16);
-        constexpr int kItemsPerThread = (kItems + kBuilders - 1) / kBuilders;  // 11
+        // items: A rows 0..127 (1024 items), then this CTA's B rows; item i ->
+        // (row group g, chunk c, row-in-group rr) with rr fastest, so 8
+        // consecutive threads store one contiguous 128-B core matrix
+        constexpr int kItems = (kM + kBRows) * (kKB / 16);
+        constexpr int kItemsPerThread = (kItems + kBuilders - 1) / kBuilders;
         Item it[kItemsPerThread];
 #pragma unroll
         for (int j = 0; j < kItemsPerThread; j++) {
@@ -250,20 +367,24 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             const bool isA = i < kM * 8;
             const int ii = isA ? i : i - kM * 8;
             const int rr = ii & 7, c = (ii >> 3) & 7, g = ii >> 6;
-            const int row = (isA ? r0 : c0) + g * 8 + rr;
+            const int lrow = g * 8 + rr;  // row inside the A or B part of the stage
+            // PAIR: B row lrow is column 256 (lrow / 128) + 128 rank + lrow % 128 of the tile
+            const int row = isA ? r0 + lrow
+                                : (PAIR ? c0 + (lrow / (kNH / 2)) * kNH + (int)rank * (kNH / 2) + lrow % (kNH / 2)
+                                        : c0 + lrow);
             it[j].dst = (isA ? 0u : (uint32_t)kAStage) + (uint32_t)((g * 8 + c) * 128 + rr * 16);
             it[j].c16 = c * 16;
             it[j].valid = inr && row < R;
             const uint32_t info = it[j].valid ? rowinfo[row] : 0u;
             const int d = (int)(info >> 8);
-            const int slot = isA ? d - rdof0 : kMaxRowDofs + d - cdof0;
+            const int slot = isA ? d - rdof0 : kMaxRowDofs + d - bdof0;
             it[j].soff = it[j].valid ? (uint32_t)(slot * kKB + c * 16) : 0u;
             it[j].t4 = (info & 0xffu) * 0x01010101u;
             if (!inr) it[j].dst = 0xffffffffu;  // no item
         }
         // Bin rows of K-block j go to ring buffer j % 4: slot k < kMaxRowDofs
         // holds DOF rdof0 + k (rows of A), slot kMaxRowDofs + k holds DOF
-        // cdof0 + k (rows of B). Every builder thread loads its share of block
+        // bdof0 + k (rows of B). Every builder thread loads its share of block
         // kb + 2 into registers before building block kb and stores it after;
         // the builders are never more than one block apart (the stage of
         // block kb + 2 frees only when every builder finished block kb), so
@@ -272,8 +393,8 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
         constexpr int kLoadsPerThread = (kLoads + kBuilders - 1) / kBuilders;
         auto load_chunk = [&](int L, int j, uint4 &v) -> bool {
             const int slot = L >> 3, c = L & 7;
-            const int d = slot < kMaxRowDofs ? rdof0 + slot : cdof0 + slot - kMaxRowDofs;
-            const bool ok = L < kLoads && (slot < kMaxRowDofs ? d <= rlast : d <= clast);
+            const int d = slot < kMaxRowDofs ? rdof0 + slot : bdof0 + slot - kMaxRowDofs;
+            const bool ok = L < kLoads && (slot < kMaxRowDofs ? d <= rlast : d <= blast);
             if (ok) v = __ldg((const uint4 *)(bins + (int64_t)d * ldb + (int64_t)j * kKB + c * 16));
             return ok;
         };
@@ -359,9 +480,14 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
                 (void)mbar_wait_bounded(smem_u32(&empty[k % kStages]), (uint32_t)((k / kStages) & 1));
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (warp == 0)
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+        if (PAIR) cluster_sync_all();  // neither CTA leaves while the pair's MMAs may read its stages
+        else __syncthreads();
+        if (warp == 0) {
+            if (PAIR)
+                asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+            else
+                asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+        }
         return;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -411,9 +537,14 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     }
     flush(-1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+    if (PAIR) cluster_sync_all();
+    else __syncthreads();
+    if (warp == 0) {
+        if (PAIR)
+            asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+        else
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+    }
     // tile partials -> per-pair accumulators (integer adds: order-independent)
     for (int i = tid; i < kMaxRowDofs * kMaxColDofs; i += kThreads) {
         const unsigned int o = ps_occ[i];
@@ -451,7 +582,7 @@ __global__ void rowinfo_kernel(const int *b2, int D, const int64_t *rowstart, ui
     for (int b = threadIdx.x; b < b2[g]; b += blockDim.x) rowinfo[rowstart[g] + b] = ((uint32_t)g << 8) | (uint32_t)b;
 }
 
-size_t smem_bytes() { return (size_t)kSmemBytes; }
+
 
 }  // namespace
 
@@ -463,18 +594,20 @@ struct OnehotPlan {
 
 static int bins_of(const SysGeom &g, int gd) { return g.bins[3 + dof_type(gd, g.nb, g.na)]; }
 
-static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles) {
+// pair: tiles of 256 rows (a CTA pair each), else 128
+static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles, bool pair = false) {
     OnehotPlan p;
     std::vector<int64_t> rs((size_t)g.D + 1, 0);
     for (int d = 0; d < g.D; d++) rs[d + 1] = rs[d] + bins_of(g, d);
     p.R = rs[g.D];
-    const int64_t mts = (p.R + kM - 1) / kM, nts = (p.R + kN - 1) / kN;
+    const int64_t tm = pair ? 2 * kM : kM;
+    const int64_t mts = (p.R + tm - 1) / tm, nts = (p.R + kN - 1) / kN;
     auto dof_at = [&](int64_t row) {  // last d with rs[d] <= row
         return (int)(std::upper_bound(rs.begin(), rs.end(), row) - rs.begin()) - 1;
     };
     int64_t cnt = 0;
     for (int64_t mt = 0; mt < mts; mt++) {
-        const int rdof0 = dof_at(mt * kM);
+        const int rdof0 = dof_at(mt * tm);
         for (int64_t nt = 0; nt < nts; nt++) {
             const int64_t cend = std::min(p.R, (nt + 1) * kN) - 1;
             if (dof_at(cend) <= rdof0) continue;  // no pair g1 < g2 in this tile
@@ -504,13 +637,22 @@ bool pairs_onehot_supported(const SysGeom &g) {
 
 size_t pairs_onehot_scratch_bytes(const SysGeom &g) { return plan(g, nullptr).total; }
 
+// CTA pairs (tcgen05.mma.cta_group::2) unless PG_ONEHOT_PAIR=0 (one CTA per
+// 128 x 512 tile). Measured at 2,994 DOFs x 100k frames, 10 bins: 38.2 ms
+// against 54.7 ms.
+static bool use_pairs() {
+    const char *e = getenv("PG_ONEHOT_PAIR");
+    return !(e && atoi(e) == 0);
+}
+
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const double *, PairOut out, int *err, cudaStream_t st, void *scratch,
                                 size_t scratch_bytes, int *launches) {
     *launches = 0;
     if (!pairs_onehot_supported(g)) return cudaErrorInvalidValue;
+    const bool pair = use_pairs();
     std::vector<TcTile> tiles;
-    const OnehotPlan p = plan(g, &tiles);
+    const OnehotPlan p = plan(g, &tiles, pair);
     if (scratch_bytes < p.total) return cudaErrorInvalidValue;
     char *base = (char *)scratch;
     std::vector<int64_t> rs((size_t)g.D + 1, 0);
@@ -532,11 +674,35 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
     rowinfo_kernel<<<g.D, 64, 0, st>>>(dof.b2, g.D, d_rs, d_ri);
     const double fix = nlogn_fix_scale(g.F);  // per-bin rounding error 2^-(s+1)
     if ((e = launch_nlogn_fix_table((unsigned long long *)d_fix, g.F, fix, st))) return e;
-    const size_t smem = smem_bytes();
-    if ((e = cudaFuncSetAttribute(onehot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
-    if (p.n_tiles > 0)
-        onehot_kernel<<<(unsigned)p.n_tiles, kThreads, smem, st>>>(bins, g.ldb, g.F, (int)p.R, d_ri, d_tiles, d_fix,
-                                                                   d_snl, d_occ, g.D, err);
+    if (p.n_tiles > 0) {
+        if (pair) {
+            const size_t smem = (size_t)OhCfg<true>::kSmemBytes;
+            if ((e = cudaFuncSetAttribute(onehot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+                return e;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)(2 * p.n_tiles));
+            cfg.blockDim = dim3(kThreads);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = 2;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            if ((e = cudaLaunchKernelEx(&cfg, onehot_kernel<true>, bins, g.ldb, g.F, (int)p.R, (const uint32_t *)d_ri,
+                                        (const TcTile *)d_tiles, (const int64_t *)d_fix, d_snl, d_occ, g.D, err)))
+                return e;
+        } else {
+            const size_t smem = (size_t)OhCfg<false>::kSmemBytes;
+            if ((e = cudaFuncSetAttribute(onehot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem)))
+                return e;
+            onehot_kernel<false><<<(unsigned)p.n_tiles, kThreads, smem, st>>>(bins, g.ldb, g.F, (int)p.R, d_ri,
+                                                                              d_tiles, d_fix, d_snl, d_occ, g.D, err);
+        }
+    }
     dim3 fg((g.D + 255) / 256, g.D);
     onehot_finalize<<<fg, 256, 0, st>>>(g, dof, d_snl, d_occ, out, log((double)g.F), fix);
     *launches = 4;
@@ -544,15 +710,16 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
 }
 
 // Form choice, from measured GB300 pair-kernel times at 2,994 DOFs x 100,000
-// frames: the histogram form takes 85.6 ms at any bin count up to 32 (32-slot
+// frames: the histogram form takes 85.8 ms at any bin count up to 32 (32-slot
 // layout, one conflict-free shared-memory reduction per update) and 117.6 ms
-// from 36 to 50 (16-slot layout); the one-hot form takes 34.9 / 45.1 / 54.6 /
-// 66.7 / 78.0 / 104.0 ms at 8 / 9 / 10 / 11 / 12 / 14 bins (B1*B2 FP8 MACs per
-// update, so its time grows as B^2). The one-hot form wins up to 12 bins.
+// from 36 to 50 (16-slot layout); the one-hot form on CTA pairs takes 24.4 /
+// 31.9 / 38.2 / 47.0 / 54.8 / 65.1 / 72.9 / 84.7 / 94.4 ms at 8 .. 16 bins
+// (B1*B2 FP8 MACs per update, so its time grows as B^2). The one-hot form
+// wins up to 15 bins.
 int autotune_form(const SysGeom &g) {
     int bmax = 0;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (pairs_onehot_supported(g) && bmax <= 12 && g.F >= 4096) return PG_FORM_ONEHOT;
+    if (pairs_onehot_supported(g) && bmax <= 15 && g.F >= 4096) return PG_FORM_ONEHOT;
     return PG_FORM_HIST;
 }
 

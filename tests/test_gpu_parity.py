@@ -174,8 +174,11 @@ def test_synthetic_matches_oracle(eng, n_atoms, F, prec, bins):
     (3, 777, 1, (20,) * 6),                          # no dihedrals
     (60, 129, 0, (12,) * 6),                         # one K-block plus one frame
 ])
-def test_onehot_form_matches_oracle(eng, n_atoms, F, prec, bins):
-    """The tcgen05 one-hot GEMM form: same S2D/MI bars and the same MIST tree."""
+@pytest.mark.parametrize("pair", ["1", "0"])
+def test_onehot_form_matches_oracle(eng, monkeypatch, n_atoms, F, prec, bins, pair):
+    """The tcgen05 one-hot GEMM form, on CTA pairs (cta_group::2, the default)
+    and on single CTAs: same S2D/MI bars and the same MIST tree."""
+    monkeypatch.setenv("PG_ONEHOT_PAIR", pair)
     t = _synth_case(n_atoms, F, prec, seed=n_atoms * 11 + F, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05)
     body = eng.entropy(t, bins, "onehot")
     assert eng.last_form() == "onehot"
