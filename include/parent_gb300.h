@@ -302,6 +302,12 @@ PG_API int pg_synth_device(pg_ctx *ctx, const pg_synth_spec *spec, void *bonds, 
  * device. It is the peak the histogram pair kernel is measured against. */
 PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s);
 
+/* Failure detection check: runs a kernel whose bounded mbarrier wait (the
+ * helper every pair kernel uses) is completed by nobody, with a limit of
+ * limit_ms. Returns PG_ERR_TIMEOUT, recorded on the device and read back as
+ * for a real timeout; the context stays usable. */
+PG_API int pg_check_wait_timeout(pg_ctx *ctx, double limit_ms);
+
 /* ------------------------------------------------------ device memory */
 
 /* Device allocations owned by the caller through the library (so callers

@@ -108,6 +108,7 @@ def lib() -> C.CDLL:
         "pg_write_mie_text": (i, [cp, i, C.POINTER(ParBodyC)]),
         "pg_write_mie_text_device": (i, [vp, cp, i, C.POINTER(ParBodyC)]),
         "pg_format_g12": (i, [C.c_double, cp]),
+        "pg_check_wait_timeout": (i, [vp, C.c_double]),
         "pg_write_mist_text": (i, [cp, i, C.POINTER(MistEdge), dp]),
         "pg_write_info_text": (i, [cp, vp]),
         "pg_synth_host": (i, [C.POINTER(SynthSpec), vp, vp, vp, i64, i]),

@@ -1218,6 +1218,19 @@ PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s) {
     return PG_OK;
 }
 
+PG_API int pg_check_wait_timeout(pg_ctx *ctx, double limit_ms) {
+    if (!ctx || !(limit_ms > 0.0) || limit_ms > 10000.0) return fail(ctx, PG_ERR_ARG, "limit_ms must be in (0, 10000]");
+    ctx->err.clear();
+    CK(cudaSetDevice(ctx->device));
+    int khz = 0;
+    CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, ctx->device));
+    CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
+    CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), ctx->stream));
+    CK(launch_wait_timeout_probe((long long)(limit_ms * (khz > 0 ? khz : 2000000)), (int *)ctx->errw.p, ctx->stream));
+    ctx->launches++;
+    return check_err_words(ctx);
+}
+
 PG_API int pg_device_alloc(pg_ctx *ctx, size_t bytes, void **ptr) {
     if (!ctx || !ptr) return fail(ctx, PG_ERR_ARG, "null argument");
     CK(cudaSetDevice(ctx->device));

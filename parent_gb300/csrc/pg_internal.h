@@ -185,6 +185,9 @@ cudaError_t launch_bat_phase(double *dtmp, int64_t ldt, int nf, int nd, const in
 // (pg_ingest.cu), else by the copy engine.
 cudaError_t h2d_copy(void *dst, const void *src, size_t bytes, cudaStream_t st, bool *pulled);
 
+// A kernel whose bounded mbarrier wait nothing completes (sets err[ERR_TIMEOUT]).
+cudaError_t launch_wait_timeout_probe(long long limit_cycles, int *err, cudaStream_t st);
+
 // MIE text on the device (pg_mie.cu): the six pair blocks of the 2D lines,
 // rows of each block in order (row0[q] .. row0[q+1]), lines numbered from
 // line0[q]; every line first goes to a 96-byte slot, then the rows are packed.

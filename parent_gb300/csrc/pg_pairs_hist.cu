@@ -467,6 +467,23 @@ cudaError_t launch_pairs_hist_batch(int bmax, const SysDesc *sys, const PairTile
     return launch_any(a, T, smem, st);
 }
 
+// A wait that nothing completes: thread 0 waits on a fresh mbarrier (one
+// expected arrival, none made) with the pair kernels' bounded wait and
+// records the timeout the way they do.
+__global__ void wait_timeout_probe(long long limit, int *err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        mbar_init_fence();
+        if (!mbar_wait_bounded(smem_u32(&bar), 0u, limit)) atomicAdd(&err[ERR_TIMEOUT], 1);
+    }
+}
+
+cudaError_t launch_wait_timeout_probe(long long limit_cycles, int *err, cudaStream_t st) {
+    wait_timeout_probe<<<1, 32, 0, st>>>(limit_cycles, err);
+    return cudaGetLastError();
+}
+
 double probe_smem_red_rate(int n_sm, cudaStream_t st, int *launches) {
     unsigned int *sink = nullptr;
     if (cudaMalloc(&sink, sizeof(unsigned int) * 2 * n_sm) != cudaSuccess) return -1.0;

@@ -49,6 +49,18 @@ def test_mist_cli_matches_reference_text(stem, tmp_path):
     assert out.read_text().splitlines() == read_text_gz(f"{stem}_ref_MIST.txt.gz")
 
 
+def test_parent_cli_host_reader_same_par(tmp_path):
+    """PG_BAT_READ=host (columns transposed on the host) writes the same .par
+    as the default device reader."""
+    import os
+    a, b = tmp_path / "dev.par", tmp_path / "host.par"
+    for out, env in ((a, dict(os.environ)), (b, dict(os.environ, PG_BAT_READ="host"))):
+        r = subprocess.run([str(BIN / "PARENT_gb300"), str(GOLDEN / "ubq_sub.bat"), str(out)] + ["50"] * 6,
+                           capture_output=True, text=True, timeout=300, env=env)
+        assert r.returncode == 0, r.stderr
+    assert a.read_bytes() == b.read_bytes()
+
+
 def test_parent_cli_form_override(tmp_path):
     """PG_FORM=onehot runs the tensor-core form through the same CLI."""
     import os

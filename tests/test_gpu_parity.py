@@ -287,6 +287,24 @@ def test_context_survives_errors(eng):
     compare_bodies(7, body, oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6))
 
 
+def test_bounded_wait_times_out_and_context_survives(eng):
+    """Failure detection without a fault: a kernel waits, with the pair
+    kernels' bounded mbarrier wait, on a barrier nobody arrives on. The wait
+    gives up after its limit, the timeout comes back as PG_ERR_TIMEOUT, and
+    the context then computes correctly (twice, to check the error word is
+    reset between calls)."""
+    import time
+    for _ in range(2):
+        t0 = time.perf_counter()
+        rc = pg.lib().pg_check_wait_timeout(eng.handle, 50.0)
+        assert rc == pg.PG_ERR_TIMEOUT
+        assert b"timed out" in pg.lib().pg_last_error(eng.handle)
+        assert time.perf_counter() - t0 < 5.0
+    t = _synth_case(10, 500, 1, seed=3)
+    body = eng.entropy(t, (50,) * 6, "hist")
+    compare_bodies(7, body, oracle.parent(t.bonds, t.angles, t.dihedrals, (50,) * 6))
+
+
 # ------------------------------------------------------------ size-independent properties
 
 def test_large_properties(eng):
