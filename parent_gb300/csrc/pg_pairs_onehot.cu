@@ -54,7 +54,6 @@ constexpr int kAStage = kM * kKB;      // 16 KB
 constexpr int kMaxRowDofs = 18, kMaxColDofs = 66;  // 2D bins >= 8
 constexpr int kBinSlots = kMaxRowDofs + kMaxColDofs;
 constexpr int kBinBufBytes = kBinSlots * kKB;      // one K-block of the tile's bin rows
-constexpr int kBinBufs = 4;                        // ring of K-block bin rows, loaded two blocks ahead
 
 // Shared-memory layout of one CTA. PAIR: a CTA pair computes a 256 x 512
 // tile with tcgen05.mma.cta_group::2 (M = 256); each CTA builds its 128 A
@@ -64,6 +63,13 @@ template <bool PAIR>
 struct OhCfg {
     static constexpr int kBRows = PAIR ? 256 : 512;  // B rows built by this CTA
     static constexpr int kStages = PAIR ? 3 : 2;
+    // Ring of K-block bin rows, loaded two blocks ahead. A builder starts
+    // block kb only when the MMAs of block kb - kStages are done, i.e. when
+    // every builder has finished that block, so the builders are at most
+    // kStages - 1 blocks apart; the buffer refilled for block kb + 2 was last
+    // read for block kb + 2 - kBinBufs, which must lie behind the slowest
+    // builder (kb - kStages + 1).
+    static constexpr int kBinBufs = kStages + 2;
     static constexpr int kBStage = kBRows * kKB;
     static constexpr int kStageBytes = kAStage + kBStage;
     // byte offsets inside the dynamic shared memory
@@ -276,7 +282,7 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             mbar_init(smem_u32(&full[k]), (PAIR && rank == 0) ? kBuilderWarps + 1 : kBuilderWarps);
             mbar_init(smem_u32(&empty[k]), 1);
         }
-        for (int k = 0; k < kBinBufs; k++) mbar_init(smem_u32(&binfull[k]), kBuilderWarps);
+        for (int k = 0; k < C::kBinBufs; k++) mbar_init(smem_u32(&binfull[k]), kBuilderWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_r0dof = (int)(rowinfo[r0 < R ? r0 : R - 1] >> 8);
         s_c0dof = (int)(rowinfo[c0 < R ? c0 : R - 1] >> 8);
@@ -297,7 +303,7 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     const int rlast = (int)(rowinfo[min(r0 + kM, R) - 1] >> 8);
     const int blast = (int)(rowinfo[min(b0 + (PAIR ? kN - kNH / 2 : kN), R) - 1] >> 8);  // last B row's DOF
     const int nkb = (F + kKB - 1) / kKB;
-    unsigned char *binbuf = smem + C::kOffBins;  // [kBinBufs][kBinSlots][kKB]
+    unsigned char *binbuf = smem + C::kOffBins;  // [C::kBinBufs][kBinSlots][kKB]
 
     if (warp == kLoaderWarp) {
         // ------------------------------------------------------- MMA issuer
@@ -382,13 +388,12 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             it[j].t4 = (info & 0xffu) * 0x01010101u;
             if (!inr) it[j].dst = 0xffffffffu;  // no item
         }
-        // Bin rows of K-block j go to ring buffer j % 4: slot k < kMaxRowDofs
-        // holds DOF rdof0 + k (rows of A), slot kMaxRowDofs + k holds DOF
-        // bdof0 + k (rows of B). Every builder thread loads its share of block
-        // kb + 2 into registers before building block kb and stores it after;
-        // the builders are never more than one block apart (the stage of
-        // block kb + 2 frees only when every builder finished block kb), so
-        // the buffer of block kb + 2 (last used by block kb - 2) is free.
+        // Bin rows of K-block j go to ring buffer j % kBinBufs: slot k <
+        // kMaxRowDofs holds DOF rdof0 + k (rows of A), slot kMaxRowDofs + k
+        // holds DOF bdof0 + k (rows of B). Every builder thread loads its share
+        // of block kb + 2 into registers before building block kb and stores
+        // it after; the ring is long enough that no builder still reads the
+        // buffer it refills (see OhCfg::kBinBufs).
         constexpr int kLoads = kBinSlots * (kKB / 16);  // 16-byte chunks per K-block
         constexpr int kLoadsPerThread = (kLoads + kBuilders - 1) / kBuilders;
         auto load_chunk = [&](int L, int j, uint4 &v) -> bool {
@@ -399,14 +404,14 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
             return ok;
         };
         auto store_block = [&](int j, const uint4 *v, const bool *ok) {
-            unsigned char *dst = binbuf + (j % kBinBufs) * kBinBufBytes;
+            unsigned char *dst = binbuf + (j % C::kBinBufs) * kBinBufBytes;
 #pragma unroll
             for (int q = 0; q < kLoadsPerThread; q++) {
                 const int L = tid + q * kBuilders;
                 if (ok[q]) *(uint4 *)(dst + (L >> 3) * kKB + (L & 7) * 16) = v[q];
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&binfull[j % kBinBufs]));
+            if (lane == 0) mbar_arrive(smem_u32(&binfull[j % C::kBinBufs]));
         };
         for (int j = 0; j < 2 && j < nkb; j++) {
             uint4 v[kLoadsPerThread];
@@ -423,14 +428,14 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
 #pragma unroll
             for (int q = 0; q < kLoadsPerThread; q++)
                 pv[q] = kb + 2 < nkb ? load_chunk(tid + q * kBuilders, kb + 2, pf[q]) : false;
-            if (!mbar_wait_bounded(smem_u32(&binfull[kb % kBinBufs]), (uint32_t)((kb / kBinBufs) & 1)) ||
+            if (!mbar_wait_bounded(smem_u32(&binfull[kb % C::kBinBufs]), (uint32_t)((kb / C::kBinBufs) & 1)) ||
                 (kb >= kStages &&
                  !mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)((kb / kStages - 1) & 1)))) {
                 s_abort = 1;
                 break;
             }
             const int nvalid = F - kb * kKB;  // frames of this block that exist (>= 1)
-            const unsigned char *bb = binbuf + (kb % kBinBufs) * kBinBufBytes;
+            const unsigned char *bb = binbuf + (kb % C::kBinBufs) * kBinBufBytes;
             unsigned char *st = stages + s * kStageBytes;
 #pragma unroll
             for (int j = 0; j < kItemsPerThread; j++) {
