@@ -434,26 +434,44 @@ PG_API int pg_bat_write_synthetic(const char *path, const pg_bat_view *v) {
               write_atoms(f, h) && (h.n_dih == 0 || wr(f, h.dih.data(), h.dih.size() * 4)) &&
               wr(f, h.masses.data(), h.masses.size() * 4);
     const size_t es = v->double_prec ? 8 : 4, nd = (size_t)h.n_dih, ld = (size_t)v->ld;
-    const size_t fbytes = 44 + (9 + 3 * nd) * es;
-    std::vector<unsigned char> fr(fbytes);
+    const size_t rec = record_bytes(h), off0 = (size_t)record_values_offset(h);
     const unsigned char *B = (const unsigned char *)v->bonds, *A = (const unsigned char *)v->angles,
                         *Dd = (const unsigned char *)v->dihedrals;
-    for (int t = 0; t < h.n_frames && ok; t++) {
-        memset(fr.data(), 0, 44 + 6 * es);
-        float time = (float)t, prec = 1000.0f;
-        memcpy(fr.data(), &time, 4);
-        memcpy(fr.data() + 4, &prec, 4);
-        unsigned char *p = fr.data() + 44 + 6 * es;
-        memcpy(p, B + (size_t)t * es, es);
-        memcpy(p + es, B + (ld + t) * es, es);
-        memcpy(p + 2 * es, A + (size_t)t * es, es);
-        p += 3 * es;
-        for (size_t d = 0; d < nd; d++, p += 3 * es) {
-            memcpy(p, B + ((d + 2) * ld + t) * es, es);
-            memcpy(p + es, A + ((d + 1) * ld + t) * es, es);
-            memcpy(p + 2 * es, Dd + (d * ld + t) * es, es);
+    const int nb = (int)nd + 2, na = (int)nd + 1, nvals = 3 + 3 * (int)nd;
+    // batches of whole records, filled by threads that own value (column)
+    // ranges and walk 64-frame blocks (the reader's transpose, reversed)
+    const size_t F = (size_t)h.n_frames, batch = std::max<size_t>(1, chunk_bytes_setting() / rec);
+    std::vector<unsigned char> buf(std::min(batch, F) * rec);
+    const int nth = reader_threads();
+    for (size_t f0 = 0; f0 < F && ok; f0 += batch) {
+        const size_t nf = std::min(batch, F - f0);
+        for (size_t i = 0; i < nf; i++) {  // time, precision, box and the 6 root externals
+            unsigned char *r = buf.data() + i * rec;
+            memset(r, 0, off0);
+            const float time = (float)(f0 + i), prec = 1000.0f;
+            memcpy(r, &time, 4);
+            memcpy(r + 4, &prec, 4);
         }
-        ok = wr(f, fr.data(), fbytes);
+        const int nt = std::min(nth, std::max(1, nvals / 32));
+        auto work = [&](int t) {
+            const int ua = (int)((int64_t)nvals * t / nt), ub = (int)((int64_t)nvals * (t + 1) / nt);
+            for (size_t i0 = 0; i0 < nf; i0 += 64) {
+                const size_t i1 = std::min(nf, i0 + 64);
+                for (int u = ua; u < ub; u++) {
+                    const size_t c = column_of_value(u, nb, na);
+                    const unsigned char *col = c < (size_t)nb ? B + c * ld * es
+                                                              : (c < (size_t)(nb + na) ? A + (c - nb) * ld * es
+                                                                                        : Dd + (c - nb - na) * ld * es);
+                    unsigned char *dst = buf.data() + off0 + (size_t)u * es;
+                    for (size_t i = i0; i < i1; i++) memcpy(dst + i * rec, col + (f0 + i) * es, es);
+                }
+            }
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nt; t++) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+        ok = wr(f, buf.data(), nf * rec);
     }
     if (fclose(f) != 0) ok = false;
     return ok ? PG_OK : ioerr(PG_ERR_IO, "AN ERROR HAS OCCURED WHILE WRITING THE FILE %s", path);
