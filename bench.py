@@ -113,6 +113,9 @@ def parse():
     ap.add_argument("--batconv", action="store_true",
                     help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
                          "with the workload's atoms and frames (host coordinates in, device columns out)")
+    ap.add_argument("--pipeline", action="store_true",
+                    help="instead of the step: write the workload as a .bat and time the drop-in CLIs on it "
+                         "(PARENT_gb300, get_PAR_MIE_gb300, get_PAR_MIST_gb300), as the reference's run.sh runs them")
     ap.add_argument("--mie", action="store_true",
                     help="instead of the step: time get_PAR_MIE's text for a .par body of the workload's size "
                          "with the host writer and with the device writer (files under $TMPDIR)")
@@ -738,10 +741,53 @@ def run_mie(args):
     return 0
 
 
+def run_pipeline(args):
+    """The reference's run.sh sequence on the drop-ins, wall clock per program:
+    PARENT_gb300 (.bat -> .par), get_PAR_MIE_gb300 (MIE text to a file),
+    get_PAR_MIST_gb300 (MIST text). Prints one JSON line."""
+    import shutil
+
+    import parent_gb300 as pg
+    n_atoms, F, prec, fbd, fbb, lat = WORKLOADS[args.workload]
+    t = pg.synth_host(n_atoms, F, double_prec=prec, seed=20260, n_latents=lat, frac_bimodal_dih=fbd,
+                      frac_bimodal_bond=fbb)
+    d = Path(tempfile.mkdtemp(prefix="pg_pipe_"))
+    bins = [str(args.bins)] * 6
+    res = {}
+    try:
+        bat, par = d / "traj.bat", d / "traj.par"
+        t0 = time.perf_counter()
+        pg.write_bat(bat, t)
+        res["write_bat_s"] = round(time.perf_counter() - t0, 2)
+        del t
+        steps = [("PARENT_gb300", [str(bat), str(par)] + bins, None),
+                 ("get_PAR_MIE_gb300", [str(par)], d / "mie.txt"),
+                 ("get_PAR_MIST_gb300", [str(par), str(d / "mist.txt")], None)]
+        for name, argv, stdout_path in steps:
+            t0 = time.perf_counter()
+            with open(stdout_path or os.devnull, "w") as out:
+                r = subprocess.run([str(pg.BIN_DIR / name)] + argv, stdout=out, stderr=subprocess.PIPE, text=True)
+            res[name + "_s"] = round(time.perf_counter() - t0, 3)
+            if r.returncode != 0:
+                raise RuntimeError(f"{name} failed: {r.stderr[-500:]}")
+        res["bat_bytes"] = bat.stat().st_size
+        res["par_bytes"] = par.stat().st_size
+        res["mie_bytes"] = (d / "mie.txt").stat().st_size
+        res["mist_lines"] = sum(1 for _ in open(d / "mist.txt"))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    print(json.dumps({"metric": "drop-in pipeline wall clock (run.sh sequence)", "results": res,
+                      "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F, "bins": args.bins,
+                                 "input": "fp64" if prec else "fp32"}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.ingest:
         return run_ingest(args)
+    if args.pipeline:
+        return run_pipeline(args)
     if args.mie:
         return run_mie(args)
     if args.batconv:
