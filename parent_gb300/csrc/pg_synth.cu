@@ -8,7 +8,7 @@
 // (pg_synth_host) and the device kernel (pg_synth_device); the two use their
 // own libm (glibc vs CUDA), so they agree in distribution, not bit-for-bit.
 //
-// Model (documented in DESIGN.md, "Synthetic workload"):
+// Model:
 //   latents  L_k(f) = phi L_k(f-1) + sqrt(1-phi^2) eta,  phi = 0.95, L_k(0) ~ N(0,1)
 //   mixing   m_g(f) = sum_k w_gk L_k(f),  w_gk ~ N(0, 0.3)
 //   bond     0.15 + 0.005 (e + m)/sqrt(1 + |w|^2)       (+0.02 in the second state of a bimodal bond)

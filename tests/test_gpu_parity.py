@@ -3,7 +3,7 @@ reference's own outputs.
 
 Bars: bin-decision inputs (per-DOF min/max/shift) and every 2D histogram
 count bit-exact; 1D/2D entropies and MI within 1e-9 nats of the FP64
-oracle (the BASELINE bar is 1e-5 nats; the decomposition error is ~1e-12);
+oracle (the required bar is 1e-5 nats; the decomposition error is ~1e-12);
 MIST edge list identical (types, indices, order), MI of each edge within
 1e-9, totals within 1e-7.
 """
@@ -19,7 +19,7 @@ from conftest import FIXTURES, GOLDEN, par_body_from_file, read_text_gz
 pytestmark = pytest.mark.gpu
 
 S_TOL = 1e-9      # nats, entropies
-MI_TOL = 1e-5     # nats, the BASELINE bar for every MI term
+MI_TOL = 1e-5     # nats, the required bar for every MI term
 
 
 @pytest.fixture(scope="module")
