@@ -143,12 +143,16 @@ static int fail(pg_ctx *c, int code, const char *fmt, ...) {
     return code;
 }
 
+// A failing runtime call also leaves its error as the thread's "last error";
+// it is cleared here so that no later launch check reports it again.
 #define CK(call)                                                                                     \
     do {                                                                                             \
         cudaError_t e_ = (call);                                                                     \
-        if (e_ != cudaSuccess)                                                                       \
+        if (e_ != cudaSuccess) {                                                                     \
+            cudaGetLastError();                                                                      \
             return fail(ctx, e_ == cudaErrorMemoryAllocation ? PG_ERR_NOMEM : PG_ERR_CUDA, "%s: %s", \
                         #call, cudaGetErrorString(e_));                                              \
+        }                                                                                            \
     } while (0)
 
 static DofArrays dof_arrays(pg_ctx *ctx, int D) {
@@ -612,6 +616,7 @@ int pg::mie_lines_device(pg_ctx *ctx, int nd, const pg_par_body *b,
                          const std::function<bool(const char *, size_t)> &sink) {
     if (!ctx || !b || nd < 0) return fail(ctx, PG_ERR_ARG, "mie: bad arguments");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     const int nb = nd + 2, na = nd + 1;
@@ -755,6 +760,7 @@ PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_devic
                                  const int *dih, int double_prec, pg_bat_view *out) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (!xyz || !dih || !out) return fail(ctx, PG_ERR_ARG, "null argument");
     if (n_dihedrals < 1 || n_frames < 1) return fail(ctx, PG_ERR_ARG, "n_dihedrals (%d) or n_frames (%d) < 1",
                                                      n_dihedrals, n_frames);
@@ -824,6 +830,7 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
                       pg_par_body *out) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (form < PG_FORM_AUTO || form > PG_FORM_ONEHOT) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
     if (traj && !traj->on_device && form != PG_FORM_ONEHOT) {
         int rc0 = setup_geometry(ctx, traj, bins);
@@ -943,6 +950,7 @@ PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins
                             int n_shards, pg_par_body *out) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (n_shards < 1 || shard < 0 || shard >= n_shards) return fail(ctx, PG_ERR_ARG, "shard %d of %d", shard, n_shards);
     if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "shards use the histogram form");
     if (form != PG_FORM_AUTO && form != PG_FORM_HIST) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
@@ -1002,6 +1010,7 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
                           int n_pairs, const int *g1, const int *g2, int64_t *counts, int64_t stride) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (n_pairs < 0 || (n_pairs > 0 && (!g1 || !g2 || !counts))) return fail(ctx, PG_ERR_ARG, "bad pair list");
     if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "count export uses the histogram form");
     int rc = run_prep(ctx, traj, bins);
@@ -1076,6 +1085,7 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
                    double totals[10]) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (!edges || !totals) return fail(ctx, PG_ERR_ARG, "null edges/totals");
     if (n_dihedrals < 0) return fail(ctx, PG_ERR_ARG, "n_dihedrals < 0");
     CK(cudaSetDevice(ctx->device));
@@ -1221,6 +1231,7 @@ PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s) {
 PG_API int pg_check_wait_timeout(pg_ctx *ctx, double limit_ms) {
     if (!ctx || !(limit_ms > 0.0) || limit_ms > 10000.0) return fail(ctx, PG_ERR_ARG, "limit_ms must be in (0, 10000]");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     CK(cudaSetDevice(ctx->device));
     int khz = 0;
     CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, ctx->device));
@@ -1297,6 +1308,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
                             pg_par_body *outs, pg_mist_edge *const *edges, double *totals) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
     ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (n_sys < 1 || !trajs || !bins) return fail(ctx, PG_ERR_ARG, "need n_sys >= 1 systems and bins");
     if (form == PG_FORM_ONEHOT)
         return fail(ctx, PG_ERR_UNSUPPORTED, "batched runs use the histogram form (the faster form at 50 bins)");

@@ -300,6 +300,7 @@ PG_API int pg_bat_read_device(const char *path, int device, pg_bat **out) {
     Header &h = b->h;
     int rc = read_bat_header(f, h, path);
     const int64_t body = rc == PG_OK ? (int64_t)ftell(f) : 0;
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     int prev = 0;
     cudaGetDevice(&prev);
     const int nst = 3;  // staging ring: read chunk k+1 while chunk k is copied and transposed

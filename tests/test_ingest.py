@@ -112,3 +112,27 @@ def test_device_reader_truncated_body(tmp_path, monkeypatch):
     # the device is still usable afterwards
     dev = pg.BatFile(GOLDEN / "synth_small.bat", device=0)
     assert dev.view().on_device == 1
+
+
+@pytest.mark.gpu
+def test_device_reader_allocation_failure(tmp_path):
+    """Allocation failure injected through the input: an FP64 header that
+    declares 2e9 frames of 24 DOFs (384 GB of columns, more than the GPU
+    holds) makes the device allocation fail; the reader returns PG_ERR_NOMEM
+    before reading the body, and the device keeps working."""
+    import struct
+    path, _ = _synthetic_bat(tmp_path, 10, 50, 1, 3)
+    raw = bytearray(path.read_bytes())
+    raw[12:16] = struct.pack("<i", 2_000_000_000)  # frames
+    path.write_bytes(bytes(raw))
+    with pytest.raises(pg.PGError) as e:
+        pg.BatFile(path, device=0)
+    assert e.value.code == pg.PG_ERR_NOMEM
+    with pg.Engine(0) as eng:
+        with pytest.raises(pg.PGError) as e2:
+            big = C.c_void_p()
+            pg._check(pg.lib().pg_device_alloc(eng.handle, 1 << 52, C.byref(big)), eng.handle)
+        assert e2.value.code == pg.PG_ERR_NOMEM
+        dev = pg.BatFile(GOLDEN / "synth_small.bat", device=0)
+        body = eng.entropy(dev.view())
+        assert np.isfinite(body.flat()).all()
