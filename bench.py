@@ -351,6 +351,7 @@ def run_batch(args):
     clk = clocks.stop()
     launches = eng.launch_count() - launches0
     graph_ms = float(eng.timings()[1])
+    batch_form = eng.last_form()  # the form the batch ran (one-hot per system where the autotuner picks it)
     sequential()
     ms_seq = timed(sequential, max(1, min(args.steps, 2)))
     value = units * world / (ms_batch / 1e3)
@@ -414,8 +415,8 @@ def run_batch(args):
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": BATCH, "systems": len(systems), "dofs": [min(Ds), max(Ds)],
                        "frames": [min(Fs), max(Fs)], "updates_per_step": units, "input": "fp32",
-                       "bins": args.bins, "form": "hist",
-                       "hist_slots": hist_slots(args.bins),
+                       "bins": args.bins, "form": batch_form,
+                       "hist_slots": hist_slots(args.bins) if batch_form == "hist" else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (total_bytes / 1e9)},
             "sequential": {"ms_per_step": ms_seq, "value": units * world / (ms_seq / 1e3),

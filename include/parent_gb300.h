@@ -171,7 +171,10 @@ PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_sh
  * list, the trees in one launch (one CTA per system), and the whole device
  * sequence is captured once into a CUDA graph that later calls with the same
  * geometry replay. outs (n_sys bodies), edges (n_sys arrays of D_s-1) and
- * totals (10 per system) may each be NULL. Histogram form only. */
+ * totals (10 per system) may each be NULL. Histogram form; with
+ * PG_FORM_AUTO and bin counts where the autotuner picks the one-hot form for
+ * every system (up to 15 bins), the systems run one after another through
+ * the one-hot form instead (same outputs). */
 PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, const int bins[6], int form,
                             pg_par_body *outs, pg_mist_edge *const *edges, double *totals);
 

@@ -1323,6 +1323,46 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     cudaStream_t st = ctx->stream;
     ctx->resident = false;
 
+    // Where the autotuner picks the one-hot form for every system (up to 15
+    // bins, long enough trajectories), that form is the faster one even
+    // without a batched launch: the systems run one after another through
+    // pg_entropy + pg_mist on this context, with the same outputs.
+    if (form == PG_FORM_AUTO) {
+        bool onehot = true;
+        for (int s = 0; s < n_sys && onehot; s++) {
+            int rc = validate_view(ctx, &trajs[s], s);
+            if (rc) return rc;
+            SysGeom g{};
+            g.n_dih = trajs[s].n_dihedrals;
+            g.nb = g.n_dih + 2;
+            g.na = g.n_dih + 1;
+            g.nd = g.n_dih;
+            g.D = g.nb + g.na + g.nd;
+            g.F = trajs[s].n_frames;
+            for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
+            onehot = autotune_form(g) == PG_FORM_ONEHOT;
+        }
+        if (onehot) {
+            for (int s = 0; s < n_sys; s++) {
+                int rc = pg_entropy(ctx, &trajs[s], bins, PG_FORM_ONEHOT, outs ? &outs[s] : nullptr);
+                if (rc) return rc;
+                if (edges || totals) {
+                    const int D = 3 * trajs[s].n_dihedrals + 3;
+                    std::vector<pg_mist_edge> e_tmp;
+                    double t_tmp[10];
+                    pg_mist_edge *e = edges ? edges[s] : nullptr;
+                    if (!e) {
+                        e_tmp.resize((size_t)std::max(D - 1, 1));
+                        e = e_tmp.data();
+                    }
+                    rc = pg_mist(ctx, trajs[s].n_dihedrals, nullptr, e, totals ? totals + 10 * (size_t)s : t_tmp);
+                    if (rc) return rc;
+                }
+            }
+            return PG_OK;
+        }
+    }
+
     // ---- layout of every system inside one arena
     std::vector<BatchLayout> sys((size_t)n_sys);
     size_t off = 0;

@@ -66,6 +66,21 @@ def test_batch_both_histogram_layouts_at_50_bins(eng, monkeypatch, slots):
     _check_against_oracle(trajs, bodies, trees, bins)
 
 
+def test_batch_at_10_bins_takes_the_onehot_form(eng):
+    """At 10 bins the autotuner picks the one-hot form for every system with
+    at least 4,096 frames: the batch runs them one by one through that form;
+    bodies and trees equal the oracle's and the single one-hot calls'."""
+    bins = (10,) * 6
+    spec = [(40, 12345, 0), (25, 5000, 1), (60, 20000, 0), (17, 4096, 0)]
+    trajs = _systems(spec, seed0=31)
+    bodies, trees = eng.entropy_batch(trajs, bins)
+    assert eng.last_form() == "onehot"
+    _check_against_oracle(trajs, bodies, trees, bins)
+    for t, b, (e, tot) in zip(trajs, bodies, trees):
+        single = eng.entropy(t, bins, "onehot")
+        assert np.array_equal(b.flat(), single.flat())
+
+
 def test_batch_equals_single_calls_bitwise(eng):
     bins = (50,) * 6
     trajs = _systems(SYSTEMS, seed0=5)
