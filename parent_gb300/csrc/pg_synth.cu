@@ -192,7 +192,7 @@ static void prepare(const pg_synth_spec &sp, std::vector<float> &lat, std::vecto
     for (int g = 0; g < D; g++) {
         sw_off[g] = (int)sw.size();
         const int type = dof_type(g, nb, na);
-        DofModel m;
+        DofModel m{};
         dof_model(sp.seed, g, type, L, sp.frac_bimodal_dih, sp.frac_bimodal_bond, m, w.data());
         if (!m.bimodal || !(sp.p_switch > 0.0)) continue;
         // geometric gaps: next switch after floor(log(u)/log(1-p)) + 1 frames
@@ -282,7 +282,7 @@ extern "C" PG_API int pg_synth_host(const pg_synth_spec *sp, void *bonds, void *
         std::vector<float> w(L > 0 ? L : 1);
         for (int g = t; g < D; g += n_threads) {
             const int type = dof_type(g, nb, na);
-            DofModel m;
+            DofModel m{};
             dof_model(sp->seed, g, type, L, sp->frac_bimodal_dih, sp->frac_bimodal_bond, m, w.data());
             void *base = type == TB ? bonds : (type == TA ? angles : dihedrals);
             const int local = g - (type == TB ? 0 : (type == TA ? nb : nb + na));
