@@ -237,6 +237,10 @@ PG_API int pg_bat_read_device(const char *path, int device, pg_bat **out);
 PG_API void pg_bat_free(pg_bat *bat);
 PG_API int pg_bat_view_of(const pg_bat *bat, pg_bat_view *view);
 PG_API int pg_bat_n_dihedrals(const pg_bat *bat);
+/* The header's dihedral table (nDih x 6 ints: atoms 1-based, type, parent
+ * dihedral 1-based or -1; read_BAT_header, io_binary.cpp:178-191), e.g. for
+ * pg_bat_from_cartesian on new coordinates of the same system. */
+PG_API int pg_bat_dihedral_table(const pg_bat *bat, int *dih);
 PG_API int pg_bat_n_frames(const pg_bat *bat);
 
 /* Writes a .bat (version 3) from DOF-major host columns with a synthetic

@@ -97,6 +97,7 @@ def lib() -> C.CDLL:
         "pg_bat_free": (None, [vp]),
         "pg_bat_view_of": (i, [vp, C.POINTER(BatView)]),
         "pg_bat_n_dihedrals": (i, [vp]),
+        "pg_bat_dihedral_table": (i, [vp, C.POINTER(C.c_int)]),
         "pg_bat_n_frames": (i, [vp]),
         "pg_bat_write_synthetic": (i, [cp, C.POINTER(BatView)]),
         "pg_par_write": (i, [cp, vp, C.POINTER(C.c_int), C.POINTER(ParBodyC)]),
@@ -431,6 +432,13 @@ class BatFile:
     @property
     def handle(self):
         return self._h
+
+    def dihedral_table(self) -> np.ndarray:
+        """The header's dihedral table, (nDih, 6) int32 (atoms 1-based, type, parent)."""
+        n = lib().pg_bat_n_dihedrals(self._h)
+        t = np.zeros((max(n, 0), 6), np.int32)
+        _check(lib().pg_bat_dihedral_table(self._h, t.ctypes.data_as(C.POINTER(C.c_int))))
+        return t
 
     def close(self):
         if self._h:

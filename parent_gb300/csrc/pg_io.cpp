@@ -418,6 +418,11 @@ PG_API int pg_bat_view_of(const pg_bat *b, pg_bat_view *v) {
     return PG_OK;
 }
 PG_API int pg_bat_n_dihedrals(const pg_bat *b) { return b ? b->h.n_dih : -1; }
+PG_API int pg_bat_dihedral_table(const pg_bat *b, int *dih) {
+    if (!b || !dih) return ioerr(PG_ERR_ARG, "pg_bat_dihedral_table: null argument");
+    if (!b->h.dih.empty()) memcpy(dih, b->h.dih.data(), b->h.dih.size() * sizeof(int));
+    return PG_OK;
+}
 PG_API int pg_bat_n_frames(const pg_bat *b) { return b ? b->h.n_frames : -1; }
 
 PG_API int pg_bat_write_synthetic(const char *path, const pg_bat_view *v) {

@@ -66,6 +66,17 @@ def test_oracle_reproduces_reference_bat_builder():
     assert np.array_equal(b, rb) and np.array_equal(a, ra) and np.array_equal(d, rd)
 
 
+def test_bat_dihedral_table_accessor():
+    """pg_bat_dihedral_table returns the header table the conversion takes:
+    the fixture's subset table maps back onto ubq_sub.bat's own atoms."""
+    bat = pg.BatFile(GOLDEN / "ubq_sub.bat")
+    tab = bat.dihedral_table()
+    assert tab.shape == (30, 6) and tab.dtype == np.int32
+    _, dih = _fixture()
+    assert np.array_equal(tab[:, 4:], dih[:, 4:])  # types and parents (atoms are renumbered in the fixture)
+    assert (tab[:, :4] >= 1).all()
+
+
 def test_oracle_rejects_bad_tables():
     xyz, dih = _fixture()
     bad = dih.copy()
