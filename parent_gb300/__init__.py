@@ -54,6 +54,22 @@ class MistEdge(C.Structure):
                 ("index_out", C.c_int), ("mi", C.c_double), ("left", C.c_int), ("pad_", C.c_int)]
 
 
+_EDGE_DTYPE = np.dtype([("type_in", "<i4"), ("type_out", "<i4"), ("index_in", "<i4"), ("index_out", "<i4"),
+                        ("mi", "<f8"), ("left", "<i4"), ("pad_", "<i4")])
+assert _EDGE_DTYPE.itemsize == C.sizeof(MistEdge)
+
+
+def _edges_array(buf, n: int) -> np.ndarray:
+    """The first n pg_mist_edge structs of a ctypes array as a numpy record
+    array (t1, t2, i1, i2, mi, left), read in place."""
+    raw = np.frombuffer(buf, dtype=_EDGE_DTYPE, count=n)
+    arr = np.empty(n, dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"), ("left", "i4")])
+    for f, g in (("t1", "type_in"), ("t2", "type_out"), ("i1", "index_in"), ("i2", "index_out"), ("mi", "mi"),
+                 ("left", "left")):
+        arr[f] = raw[g]
+    return arr
+
+
 class SynthSpec(C.Structure):
     _fields_ = [("n_atoms", C.c_int), ("n_frames", C.c_int), ("double_prec", C.c_int),
                 ("n_latents", C.c_int), ("seed", C.c_uint64), ("frac_bimodal_dih", C.c_double),
@@ -293,9 +309,7 @@ class Engine:
         totals = (C.c_double * 10)()
         bc = body.c() if body is not None else None
         _check(lib().pg_mist(self._ctx, n_dih, C.byref(bc) if bc else None, edges, totals), self._ctx)
-        arr = np.array([(e.type_in, e.type_out, e.index_in, e.index_out, e.mi, e.left) for e in edges[:n]],
-                       dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"), ("left", "i4")])
-        return arr, np.array(totals[:], dtype=np.float64)
+        return _edges_array(edges, n), np.array(totals[:], dtype=np.float64)
 
     def entropy_batch(self, trajs, bins=(50,) * 6, form: str | int = "auto", bodies: bool = True,
                       trees: bool = True):
@@ -324,11 +338,7 @@ class Engine:
         if trees:
             res = []
             for k, (v, e) in enumerate(zip(views, ebufs)):
-                m = 3 * v.n_dihedrals + 2
-                a = np.array([(x.type_in, x.type_out, x.index_in, x.index_out, x.mi, x.left) for x in e[:m]],
-                             dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"),
-                                    ("left", "i4")])
-                res.append((a, totals[10 * k:10 * k + 10].copy()))
+                res.append((_edges_array(e, 3 * v.n_dihedrals + 2), totals[10 * k:10 * k + 10].copy()))
         return outs, res
 
     def entropy_shard(self, traj: Trajectory | BatView, bins, shard: int, n_shards: int,

@@ -131,6 +131,19 @@ struct pg_ctx {
     DevBuf bc_out, bc_stage, bc_soa, bc_tmp, bc_tab;
     // MIE text: body, line slots and lengths, row offsets, text, host fallbacks
     DevBuf mie_body, mie_slots, mie_lens, mie_rows, mie_text, mie_fb;
+    // pinned host staging for small results (MIST edges, 1D entropies)
+    void *hstage = nullptr;
+    size_t hstage_n = 0;
+    cudaError_t ensure_hstage(size_t bytes) {
+        if (bytes <= hstage_n && hstage) return cudaSuccess;
+        if (hstage) cudaFreeHost(hstage);
+        hstage = nullptr;
+        hstage_n = 0;
+        const size_t b = std::max<size_t>(bytes, 4096);
+        cudaError_t e = cudaHostAlloc(&hstage, b, cudaHostAllocDefault);
+        if (e == cudaSuccess) hstage_n = b;
+        return e;
+    }
 };
 
 static int fail(pg_ctx *c, int code, const char *fmt, ...) {
@@ -598,6 +611,7 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     }
     for (auto &e : ctx->pev)
         if (e) cudaEventDestroy(e);
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
     delete ctx;
 }
 
@@ -1093,6 +1107,10 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     const int nb = n_dihedrals + 2, na = n_dihedrals + 1, nd = n_dihedrals, D = nb + na + nd;
     const ParLayout L = par_layout(n_dihedrals);
     std::vector<double> s1((size_t)D);
+    // results come back through one pinned buffer: s1 | edge MI | from | to
+    CK(ctx->ensure_hstage((size_t)D * (2 * sizeof(double) + 2 * sizeof(int)) + 64));
+    double *h_s1 = (double *)ctx->hstage, *hmi = h_s1 + D;
+    int *hf = (int *)(hmi + D), *ht = hf + D;
     CK(cudaEventRecord(ctx->ev[0], st));
     if (body) {
         const double *src[9] = {body->s1_b, body->s1_a, body->s1_d, body->bb, body->ba, body->bd, body->aa, body->ad, body->dd};
@@ -1115,8 +1133,6 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     } else {
         if (!ctx->resident || ctx->geo.n_dih != n_dihedrals)
             return fail(ctx, PG_ERR_ARG, "no resident MI matrix for %d dihedrals", n_dihedrals);
-        CK(cudaMemcpyAsync(s1.data(), dof_arrays(ctx, D).s1, (size_t)D * sizeof(double),
-                           cudaMemcpyDeviceToHost, st));
     }
     CK(ctx->edges.ensure((size_t)D * (sizeof(double) + 2 * sizeof(int)) + 256));
     CK(ctx->mistscr.ensure(mist_scratch_bytes(D)));
@@ -1126,21 +1142,22 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     CK(launch_mist_impl(D, nb, na, (const double *)ctx->mi.p, ctx->mistscr.p, emi, efrom, eto, st));
     ctx->launches++;
     CK(cudaEventRecord(ctx->ev[2], st));
-    std::vector<double> hmi((size_t)D);
-    std::vector<int> hf((size_t)D), ht((size_t)D);
+    if (!body)
+        CK(cudaMemcpyAsync(h_s1, dof_arrays(ctx, D).s1, (size_t)D * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (D > 1) {
-        CK(cudaMemcpyAsync(hmi.data(), emi, (size_t)(D - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hf.data(), efrom, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(ht.data(), eto, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hmi, emi, (size_t)(D - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hf, efrom, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(ht, eto, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
     }
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(cudaStreamSynchronize(st));
+    if (!body) memcpy(s1.data(), h_s1, (size_t)D * sizeof(double));
     float ms[3];
     cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);
     cudaEventElapsedTime(&ms[2], ctx->ev[2], ctx->ev[3]);
     ctx->timings[2] = ms[1];
-    return mist_edges_to_user(ctx, n_dihedrals, hmi.data(), hf.data(), ht.data(), s1.data(), edges, totals);
+    return mist_edges_to_user(ctx, n_dihedrals, hmi, hf, ht, s1.data(), edges, totals);
 }
 
 }  // extern "C"
