@@ -251,6 +251,23 @@ def test_mist_tie_order_matches_reference_scan(eng, seed):
 
 # ------------------------------------------------------------ error paths
 
+@pytest.mark.parametrize("cluster", ["1", "0"])
+def test_mist_over_a_cluster_matches_oracle(eng, monkeypatch, cluster):
+    """1,194 DOFs: Prim over a cluster of 8 CTAs (the default from 1,024
+    vertices) and over one CTA give the oracle's edge list on the same .par
+    body, in the reference's tie order."""
+    monkeypatch.setenv("PG_MIST_CLUSTER", cluster)
+    n_atoms = 400
+    t = _synth_case(n_atoms, 3000, 0, seed=17, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05)
+    body = eng.entropy(t, (20,) * 6, "hist")
+    n = n_atoms - 3
+    re, rt = oracle.mist(n, body.blocks)
+    e2, tot2 = eng.mist(n)  # on the MI matrix the entropy call left on the device
+    compare_mist(e2, tot2, re, rt)
+    e, tot = eng.mist(n, body)  # from the .par body
+    compare_mist(e, tot, re, rt)
+
+
 def test_negative_bond_is_rejected(eng):
     t = _synth_case(10, 500, 1, seed=1)
     t.bonds[3, 17] = -0.1
