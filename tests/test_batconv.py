@@ -157,3 +157,25 @@ def test_gpu_conversion_rejects_bad_tables():
             eng.bat_from_cartesian(xyz, bad)
         v = eng.bat_from_cartesian(xyz, dih)  # the context is still usable
         assert v.on_device == 1
+
+
+@pytest.mark.gpu
+def test_gpu_conversion_from_device_coordinates():
+    """xyz_on_device = 1: coordinates already in device memory give the same
+    columns as the host-array call."""
+    import ctypes as C
+
+    import torch
+    xyz, dih = _chain(31, 5000, seed=9)
+    with pg.Engine(0) as eng:
+        want = [c.copy() for c in _cols(eng.bat_from_cartesian(xyz, dih, double_prec=1))]
+        dx = torch.from_numpy(xyz).cuda().contiguous()
+        torch.cuda.synchronize()
+        v = pg.BatView()
+        d = np.ascontiguousarray(dih, dtype=np.int32)
+        rc = pg.lib().pg_bat_from_cartesian(eng.handle, C.c_void_p(dx.data_ptr()), 1, xyz.shape[0], dih.shape[0],
+                                            d.ctypes.data_as(C.POINTER(C.c_int)), 1, C.byref(v))
+        assert rc == pg.PG_OK
+        got = _cols(v)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)

@@ -268,6 +268,17 @@ def test_mist_over_a_cluster_matches_oracle(eng, monkeypatch, cluster):
     compare_mist(e, tot, re, rt)
 
 
+@pytest.mark.parametrize("groups", ["4", "16"])
+def test_grouped_upload_schedule_matches(eng, monkeypatch, groups):
+    """PG_STREAM_GROUPS > 1 (uploads in DOF groups on the copy stream, pair
+    launches alternating between two streams) gives the same body, bit for
+    bit, as the default one-group upload."""
+    t = _synth_case(150, 6000, 0, seed=23, frac_bimodal_dih=0.2)
+    base = eng.entropy(t, (50,) * 6, "hist").flat()
+    monkeypatch.setenv("PG_STREAM_GROUPS", groups)
+    assert np.array_equal(eng.entropy(t, (50,) * 6, "hist").flat(), base)
+
+
 def test_negative_bond_is_rejected(eng):
     t = _synth_case(10, 500, 1, seed=1)
     t.bonds[3, 17] = -0.1
