@@ -197,7 +197,7 @@ def cpu_sample(args, wl):
     ref = oracle.parent(t.bonds, t.angles, t.dihedrals, (args.bins,) * 6)
     dt = time.perf_counter() - t0
     sample = f"{D} DOFs ({na} atoms) x {F} frames of the same generator, {units:.3e} updates, {dt:.2f} s"
-    cpu_sample.last = (t, ref)  # the checker's result on the sample, for parity_on_sample
+    cpu_sample.last = (t, ref)  # the oracle's result on the sample, for parity_on_sample
     return units / dt, sample, threads, dt
 
 
@@ -221,7 +221,7 @@ def _mutual_all(n: int, body: dict):
 
 
 def parity_on_sample(eng, bins, form):
-    """The GPU path on the CPU baseline's sample against the checker's FP64
+    """The GPU path on the CPU baseline's sample against the oracle's FP64
     result there: the largest |dS| and |dMI| (nats) over every term."""
     import numpy as np
     t, ref = cpu_sample.last

@@ -4,7 +4,7 @@ ctypes access to oracle/liboracle.so, the plain-C restatement of the
 reference PARENT algorithm (oracle/parent_oracle.c), and to the reference
 programs compiled from their own sources into oracle/_ref/ when this machine
 has them. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-leg import this module, and only as the checker or the timed CPU reference;
+leg import this module, and only to check results or as the timed CPU reference;
 the product (parent_gb300) never loads it.
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 /*
  * ORACLE — test infrastructure only. Nothing in the product links, loads or
  * calls this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg use it, and only as the checker / the timed CPU reference.
+ * baseline leg use it, and only to check results or as the timed CPU reference.
  *
  * A plain-C restatement of the reference PARENT algorithm (markusfleck/PARENT):
  * .bat parsing, per-DOF extrema and dihedral "modfit" shift, 1D and 2D
