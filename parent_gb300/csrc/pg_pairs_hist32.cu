@@ -61,7 +61,8 @@ constexpr int kConsumerThreads = kConsumers * 32;
 constexpr int kRows = 4, kCols = 8;        // tile: 4 row DOFs x 8 column DOFs
 constexpr int kNRow = kRows + kCols;       // staged bin rows per chunk
 constexpr int kMaxStages = 6;
-constexpr int kPad = 32;                   // bytes between staged rows
+constexpr int kPad = 16;                   // bytes between staged rows: a row stride of an odd number of
+                                           // 16-byte units puts the 8 column rows of a stage on distinct banks
 constexpr int kFoldFrames = 32768;         // counts moved out per fold; frames between folds
 constexpr int kBmax16 = 50;                // 16-bit: 32 lanes x 1,250 words x 4 B = 160 KB of counters
 constexpr int kBmax32 = 35;                // 32-bit: 32 lanes x 1,225 words x 4 B = 157 KB
