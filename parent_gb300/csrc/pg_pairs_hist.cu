@@ -209,12 +209,14 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist_kernel(const __grid_co
                 const unsigned char *rrow = stage + (size_t)(st * NROW + pr) * fcs;
                 const unsigned char *crow = stage + (size_t)(st * NROW + T + pc) * fcs;
                 if (valid) {
-                    for (int off = g0 * 16; off < fvalid; off += S * 16) {
+                    const int fend = fvalid & ~15;  // frames in whole 16-frame groups
+                    int off = g0 * 16;
+                    for (; off < fend; off += S * 16) {
                         const uint4 rv = *(const uint4 *)(rrow + off);
                         const uint4 cv = *(const uint4 *)(crow + off);
                         const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
                         const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
-                        if (off + 16 <= fvalid) {
+                        {
                             // two frames per 32-bit IMAD: bytes spread into
                             // 16-bit halves, idx = br*Bc + bc < 65536 never
                             // carries across
@@ -235,7 +237,14 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist_kernel(const __grid_co
                                     red_add1_at(hbase + (((k & 1) ? (v >> 16) : (v & 0xffffu)) << SH));
                                 }
                             }
-                        } else {  // ragged end of the trajectory
+                        }
+                    }
+                    if (off < fvalid) {  // the ragged last group of the trajectory (off == fend)
+                        const uint4 rv = *(const uint4 *)(rrow + off);
+                        const uint4 cv = *(const uint4 *)(crow + off);
+                        const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                        const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                        {
                             const int n = fvalid - off;
 #pragma unroll
                             for (int k = 0; k < 16; k++) {

@@ -232,12 +232,14 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                     const unsigned char *rrow = stage + (size_t)(st * kNRow + pr) * fcs;
                     const unsigned char *crow = stage + (size_t)(st * kNRow + kRows + pc) * fcs;
                     if (valid) {
-                        for (int off = g0 * 16; off < fvalid; off += kConsumers * 16) {
+                        const int fend = fvalid & ~15;  // frames in whole 16-frame groups
+                        int off = g0 * 16;
+                        for (; off < fend; off += kConsumers * 16) {
                             const uint4 rv = *(const uint4 *)(rrow + off);
                             const uint4 cv = *(const uint4 *)(crow + off);
                             const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
                             const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
-                            if (off + 16 <= fvalid) {
+                            {
                                 if (W32) {
                                     // word addresses hbase + 128 idx for the 16 frames, with
                                     // the multiplies on the FMA pipe (multipliers come from
@@ -284,7 +286,14 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
                                         }
                                     }
                                 }
-                            } else {  // ragged end of the trajectory
+                            }
+                        }
+                        if (off < fvalid) {  // the ragged last group of the trajectory (off == fend)
+                            const uint4 rv = *(const uint4 *)(rrow + off);
+                            const uint4 cv = *(const uint4 *)(crow + off);
+                            const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                            const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                            {
                                 const int n = fvalid - off;
 #pragma unroll
                                 for (int k = 0; k < 16; k++) {

@@ -39,8 +39,10 @@ __device__ __forceinline__ void mbar_arrive_relaxed(uint32_t bar) {
     asm volatile("mbarrier.arrive.relaxed.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 // Bounded wait: gives up after `limit` cycles (kWaitCycles by default) and
-// returns false.
+// returns false. The first test runs before the clock is read: a stage that
+// is already there costs one test.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit = kWaitCycles) {
+    if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (clock64() - t0 > limit) return false;
