@@ -108,7 +108,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample-atoms", type=int, default=0,
                     help="atoms of the bounded DOF sample timed on the host cores "
-                         "(0: sized to ~2.5e10 pair-frame updates, about 10 s on 16 cores)")
+                         "(0: sized to ~8e10 pair-frame updates, about 10 s on 16 Grace cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batconv", action="store_true",
                     help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
@@ -187,7 +187,7 @@ def cpu_sample(args, wl):
     import parent_gb300 as pg
     na = args.cpu_sample_atoms
     if na <= 0:
-        dofs = int((2 * 2.5e10 / F) ** 0.5)
+        dofs = int((2 * 8e10 / F) ** 0.5)
         na = max(6, min(n_atoms, dofs // 3 + 2))
     t = pg.synth_host(na, F, double_prec=prec, seed=1234, n_latents=lat, frac_bimodal_dih=fbd,
                       frac_bimodal_bond=fbb)
