@@ -110,6 +110,10 @@ def parse():
                     help="atoms of the bounded DOF sample timed on the host cores "
                          "(0: sized to ~8e10 pair-frame updates, about 10 s on 16 Grace cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--parity-pairs", type=int, default=10000,
+                    help="pairs of the timed system checked against the FP64 oracle after the timed region "
+                         "(plus bit-exact counts on 100 of them and the oracle's MIST on the GPU's body)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size parity leg")
     ap.add_argument("--batconv", action="store_true",
                     help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
                          "with the workload's atoms and frames (host coordinates in, device columns out)")
@@ -501,14 +505,18 @@ def run_gb300(args):
     value = units * world / (ms_total / 1e3 / args.steps)
 
     # ---- end to end through the public API, pinned host buffers
+    import ctypes as C
+    import numpy as np
     e2e = None
-    if args.e2e_steps > 0:
-        import ctypes as C
-        import numpy as np
+    want_parity = rank == 0 and world == 1 and not args.no_parity and args.parity_pairs > 0
+    host = None
+    if args.e2e_steps > 0 or want_parity:
+        # the step's input columns in pinned host memory (bonds | angles | dihedrals)
         host = pg.C.c_void_p()
         pg._check(pg.lib().pg_host_alloc_pinned(D * F * es, C.byref(host)))
         eng.memcpy(host.value, dbuf, D * F * es, 2)
         eng.synchronize()
+    if args.e2e_steps > 0:
         hview = pg.BatView(n_dih, F, prec, 0, F, host.value, host.value + nb * F * es,
                            host.value + (nb + na) * F * es)
         sizes = pg.block_sizes(n_dih)
@@ -543,8 +551,14 @@ def run_gb300(args):
         e2e = {"value": units * world / sec, "unit": UNIT, "h2d_bytes_per_step": D * F * es,
                "d2h_bytes_per_step": total * 8 + (D - 1) * (4 * 4 + 8 + 8), "ms_per_step": sec * 1e3,
                "breakdown": parts[-1]}
-        pg._check(pg.lib().pg_host_free_pinned(host))
         pg._check(pg.lib().pg_host_free_pinned(hout))
+
+    # ---- full-size parity of the timed system itself (outside every timed region)
+    parity_full = None
+    if want_parity:
+        parity_full = full_parity(args, eng, view, host.value, n_dih, F, prec, bins)
+    if host is not None:
+        pg._check(pg.lib().pg_host_free_pinned(host))
 
     # ---- roofline of the dominant kernel (the pair kernel)
     peaks = {}
@@ -595,7 +609,8 @@ def run_gb300(args):
             "kernel_ms": {"prep": statistics.mean(prep_ms), "pairs": statistics.mean(pair_ms),
                           "mist": statistics.mean(mist_ms)},
             "roofline": roofline, "roofline_prep": roofline_prep,
-            "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "cpu_baseline": cpu, "parity": parity_full, "parity_cpu_sample": parity, "e2e": e2e,
+            "gpu_launches": launches, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
     eng.free(dbuf)
@@ -603,6 +618,39 @@ def run_gb300(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def full_parity(args, eng, view, host_ptr: int, n_dih: int, F: int, prec: int, bins):
+    """The timed system itself against the FP64 oracle: one more pg_entropy +
+    pg_mist on the device-resident columns (the same call the timed steps
+    make), then oracle.check.check_run on the host copy of the same columns:
+    args.parity_pairs random pairs (S2D and MI terms), bit-exact counts on
+    100 of them (pg_pair_counts, the histogram kernel), every 1D entropy, and
+    the oracle's MIST (the reference's scan order) on the GPU's own body,
+    which must reproduce the GPU's edge list."""
+    import ctypes as C
+    import numpy as np
+    import parent_gb300 as pg
+    from oracle import check
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    body = eng.entropy(view, bins, args.form)
+    form = eng.last_form()
+    edges, _ = eng.mist(n_dih)
+    nb, na = n_dih + 2, n_dih + 1
+    D = nb + na + n_dih
+    dt = np.float64 if prec else np.float32
+    flat = np.ctypeslib.as_array(C.cast(host_ptr, C.POINTER(C.c_double if prec else C.c_float)), (D * F,))
+    cols = flat.reshape(D, F)
+    b, a, d = cols[:nb], cols[nb:nb + na], cols[nb + na:]
+    t0 = time.perf_counter()
+    res = check.check_run(b, a, d, bins, body.blocks, edges,
+                          gpu_counts=lambda pairs: eng.pair_counts(view, bins, pairs),
+                          n_pairs=args.parity_pairs, n_count_pairs=100)
+    res.update({"form": form, "counts_form": "hist", "oracle_threads": threads,
+                "oracle_s": round(time.perf_counter() - t0, 2), "input": str(np.dtype(dt)),
+                "system": "the timed system (same seed, columns and bins)"})
+    return res
 
 
 def run_ingest(args):

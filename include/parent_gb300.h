@@ -139,11 +139,15 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
  * pg_mist produces them. stream: a cudaStream_t (NULL = default stream); the
  * call only enqueues, results are ready when the stream reaches them.
  * D must not exceed PG_NOALLOC_MAX_DOFS (PG_ERR_UNSUPPORTED otherwise). The
- * per-DOF scratch is one static device array per GPU (16 bytes x
- * PG_NOALLOC_MAX_DOFS, held until exit) shared by every call: calls that
- * overlap on the GPU race on it and must be serialised by the caller. The
- * first call on a device looks up that array's address; make that first call
- * before any stream capture. */
+ * per-DOF scratch of the one-CTA kernel, when it runs on more DOFs than its
+ * shared memory holds (above 12,800 DOFs with PG_MIST_CLUSTER=0), is one
+ * static device array per GPU (16 bytes x PG_NOALLOC_MAX_DOFS, held until
+ * exit) shared by every call: such calls that overlap on the GPU race on it
+ * and must be serialised by the caller. The other kernels keep their
+ * per-DOF arrays in shared memory. Every call looks up that array's address
+ * with the current device (after a device reset too); the first call on a
+ * device may also load the library's device code, so make it before any
+ * stream capture. */
 #define PG_NOALLOC_MAX_DOFS 16384
 PG_API int pg_mist_noalloc(int n_dihedrals, const double *mi, double *edge_mi, int *edge_from,
                            int *edge_to, void *stream);

@@ -10,6 +10,7 @@ the product (parent_gb300) never loads it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -20,6 +21,16 @@ LIB = HERE / "liboracle.so"
 REF = HERE / "_ref"
 
 _lib = None
+
+
+def reference_root() -> Path:
+    """Where the reference project's sources are (PG_REFERENCE_ROOT, else the
+    oracle build recipe's REF_ROOT); the directory may not exist."""
+    env = os.environ.get("PG_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref-root"], capture_output=True, text=True)
+    return Path(r.stdout.strip() or ".") if r.returncode == 0 else Path(".")
 
 
 def build() -> Path:
@@ -46,6 +57,9 @@ def lib() -> C.CDLL:
         L.or_mutual.argtypes = [i, i, i, i] + [dp] * 9
         L.or_mie_totals.argtypes = [i] + [dp] * 9 + [dp]
         L.or_mist.argtypes = [i] + [dp] * 9 + [ip, ip, ip, ip, dp, ip, dp]
+        L.or_mist_gap.argtypes = [i] + [dp] * 9 + [ip, ip, ip, ip, dp, ip, dp, dp]
+        L.or_sample.argtypes = [i, i, i, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, ip, i, ip, ip,
+                                dp, dp, i, C.POINTER(C.c_int64), C.c_longlong, dp, dp, dp]
         L.or_bat_from_xyz.argtypes = [i, i, C.POINTER(C.c_float), ip, dp, dp, dp]
         _lib = L
     return _lib
@@ -142,18 +156,60 @@ def mie_totals(n_dih: int, body: dict) -> np.ndarray:
     return t
 
 
-def mist(n_dih: int, body: dict):
-    """(edges structured array, totals[10]) with the reference's one-thread scan order."""
+def mist(n_dih: int, body: dict, gaps: bool = False):
+    """(edges structured array, totals[10]) with the reference's one-thread scan
+    order; with gaps=True also each step's gap between the winning MI and the
+    largest other candidate (0 where the scan order decided among equal values)."""
     n = 3 * n_dih + 2
     t1, t2, i1, i2, left = (np.zeros(max(n, 1), dtype=np.int32) for _ in range(5))
     mi = np.zeros(max(n, 1))
+    gap = np.zeros(max(n, 1))
     tot = np.zeros(10)
     ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
-    lib().or_mist(n_dih, *[_p(np.ascontiguousarray(body[k], dtype=np.float64)) for k in BLOCKS],
-                  ip(t1), ip(t2), ip(i1), ip(i2), _p(mi), ip(left), _p(tot))
+    lib().or_mist_gap(n_dih, *[_p(np.ascontiguousarray(body[k], dtype=np.float64)) for k in BLOCKS],
+                      ip(t1), ip(t2), ip(i1), ip(i2), _p(mi), ip(left), _p(gap), _p(tot))
     arr = np.zeros(n, dtype=[("t1", "i4"), ("t2", "i4"), ("i1", "i4"), ("i2", "i4"), ("mi", "f8"), ("left", "i4")])
     arr["t1"], arr["t2"], arr["i1"], arr["i2"], arr["mi"], arr["left"] = t1[:n], t2[:n], i1[:n], i2[:n], mi[:n], left[:n]
+    if gaps:
+        return arr, tot, gap[:n]
     return arr, tot
+
+
+def sample(bonds, angles, dihedrals, bins, g1, g2, n_counts: int = 0):
+    """The oracle at full size on a sample of pairs, without an FP64 copy of the
+    trajectory: per-DOF (s1, min, max, modfit) for every DOF and the 2D entropy
+    (and, for the first n_counts pairs, the B1 x B2 int64 counts) of each pair
+    g1[k] < g2[k] (global DOF indices). Columns: 2D arrays (rows = DOFs of one
+    type), float32 or float64, C-contiguous, frames along axis 1."""
+    cols = [np.asarray(x) for x in (bonds, angles, dihedrals)]
+    dt = cols[0].dtype
+    if dt not in (np.float32, np.float64) or any(c.dtype != dt or not c.flags.c_contiguous for c in cols):
+        raise ValueError("columns must be C-contiguous float32 or float64 of one dtype")
+    nd = cols[2].shape[0]
+    F = cols[0].shape[1]
+    D = 3 * nd + 3
+    g1 = np.ascontiguousarray(g1, dtype=np.int32)
+    g2 = np.ascontiguousarray(g2, dtype=np.int32)
+    s1, mn, mx, mf = (np.zeros(D) for _ in range(4))
+    s2 = np.zeros(max(len(g1), 1))
+    bmax = max(bins[3:])
+    cnt = np.zeros((max(n_counts, 1), bmax * bmax), dtype=np.int64)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    # an empty dihedral block still needs a valid pointer
+    dptr = cols[2].ctypes.data if nd > 0 else cols[1].ctypes.data
+    rc = lib().or_sample(nd, F, 1 if dt == np.float64 else 0, cols[0].ctypes.data, cols[1].ctypes.data, dptr,
+                         F, ip(np.ascontiguousarray(bins, dtype=np.int32)), len(g1), ip(g1), ip(g2), _p(s1),
+                         _p(s2), n_counts, cnt.ctypes.data_as(C.POINTER(C.c_int64)), bmax * bmax,
+                         _p(mn), _p(mx), _p(mf))
+    if rc:
+        raise RuntimeError(f"oracle rejected the input (code {rc})")
+    counts = []
+    for k in range(n_counts):
+        t1 = 0 if g1[k] < nd + 2 else (1 if g1[k] < 2 * nd + 3 else 2)
+        t2 = 0 if g2[k] < nd + 2 else (1 if g2[k] < 2 * nd + 3 else 2)
+        B1, B2 = bins[3 + t1], bins[3 + t2]
+        counts.append(cnt[k, :B1 * B2].reshape(B1, B2).copy())
+    return {"s1": s1, "s2": s2[:len(g1)], "min": mn, "max": mx, "modfit": mf, "counts": counts}
 
 
 def fmt12(x: float) -> str:

@@ -13,6 +13,15 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef _OPENMP
+#include <omp.h>
+static int omp_nthreads(void) { return omp_get_num_threads(); }
+static int omp_thread(void) { return omp_get_thread_num(); }
+#else
+static int omp_nthreads(void) { return 1; }
+static int omp_thread(void) { return 0; }
+#endif
+
 #define MODFITNBINS 100 /* PARENT.cpp:51 */
 
 void or_free(void *p) { free(p); }
@@ -76,6 +85,108 @@ int or_read_bat(const char *path, int *n_dihedrals, int *n_frames, int *double_p
 
 /* ---------------------------------------------------------------- extrema */
 
+/* One bond column, PARENT.cpp:511-536. Returns 1 for a negative bond. */
+static int ext_bond(const double *x, size_t F, double *mn, double *mx) {
+    double tmpMax = -1.0e100, tmpMin = 1.0e100;
+    for (size_t i = 0; i < F; i++) {
+        if (x[i] > tmpMax) tmpMax = x[i];
+        if (x[i] < tmpMin) tmpMin = x[i];
+    }
+    const int bad = (tmpMin < 0.0) || (tmpMax < 0.0);
+    tmpMin -= 0.000000005;
+    tmpMax += 0.000000005;
+    if (tmpMin < 0.0) tmpMin = 0.0;
+    if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
+    *mx = tmpMax;
+    *mn = tmpMin;
+    return bad;
+}
+
+/* One angle column, PARENT.cpp:538-562. */
+static void ext_angle(const double *x, size_t F, double pi, double *mn, double *mx) {
+    double tmpMax = -1.0e100, tmpMin = 1.0e100;
+    for (size_t i = 0; i < F; i++) {
+        if (x[i] > tmpMax) tmpMax = x[i];
+        if (x[i] < tmpMin) tmpMin = x[i];
+    }
+    tmpMin -= 0.000000005;
+    tmpMax += 0.000000005;
+    if (tmpMin < 0) tmpMin = 0;
+    if (tmpMax > pi) tmpMax = pi;
+    if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
+    *mx = tmpMax;
+    *mn = tmpMin;
+}
+
+/* The periodic shift of one dihedral value, PARENT.cpp:611. */
+static inline double dih_shift(double x, double modFit, double pi) {
+    return x + modFit - 2 * pi * (int)((x + modFit) / (2 * pi));
+}
+
+/* One dihedral column, PARENT.cpp:564-637: the shift ("modfit") is found
+ * from a 100-bin occupancy histogram and applied in place, then the extrema
+ * of the shifted column. Returns the number of out-of-range histogram
+ * indices (undefined behaviour in the reference). */
+static int ext_dih(double *x, size_t F, double pi, double *mn, double *mx, double *modfit) {
+    int bad = 0;
+    long long histo[MODFITNBINS];
+    for (int k = 0; k < MODFITNBINS; k++) histo[k] = 0;
+    const double binsize = (2 * pi + 0.000000005) / MODFITNBINS;
+    for (size_t i = 0; i < F; i++) {
+        int idx = (int)((x[i]) / binsize);
+        if (idx < 0 || idx >= MODFITNBINS) { bad++; idx = idx < 0 ? 0 : MODFITNBINS - 1; }
+        histo[idx] += 1;
+    }
+    int zeroExists = 0;
+    for (int k = 0; k < MODFITNBINS; k++) zeroExists = zeroExists || (histo[k] == 0);
+    int longestZeroStretch, longestZeroStretchPos, currentZeroStretch, currentZeroStretchPos = 0;
+    if (zeroExists) {
+        longestZeroStretch = 0;
+        currentZeroStretch = 0;
+        longestZeroStretchPos = -1;
+        for (int k = 0; k < 2 * MODFITNBINS; k++) {
+            int l = k % MODFITNBINS;
+            if ((currentZeroStretch == 0) && (histo[l] == 0)) {
+                currentZeroStretch = 1;
+                currentZeroStretchPos = k;
+            }
+            if ((currentZeroStretch > 0) && (histo[l] == 0)) currentZeroStretch += 1;
+            if ((currentZeroStretch > 0) && (histo[l] != 0)) {
+                if (currentZeroStretch > longestZeroStretch) {
+                    longestZeroStretch = currentZeroStretch;
+                    longestZeroStretchPos = currentZeroStretchPos;
+                }
+                currentZeroStretch = 0;
+            }
+        }
+    } else {
+        longestZeroStretchPos = 0;
+        longestZeroStretch = (int)histo[0];
+        for (int k = 0; k < MODFITNBINS; k++) {
+            if (histo[k] < longestZeroStretch) {
+                longestZeroStretch = (int)histo[k];
+                longestZeroStretchPos = k;
+            }
+        }
+    }
+    const double modFit = 2 * pi - (longestZeroStretchPos + 0.5) * binsize;
+    if (modfit) *modfit = modFit;
+    for (size_t k = 0; k < F; k++) x[k] = dih_shift(x[k], modFit, pi);
+    double tmpMax = -1.0e100, tmpMin = 1.0e100;
+    for (size_t i = 0; i < F; i++) {
+        if (x[i] > tmpMax) tmpMax = x[i];
+        if (x[i] < tmpMin) tmpMin = x[i];
+    }
+    tmpMin -= 0.000000005;
+    tmpMax += 0.000000005;
+    if (tmpMin < 0.0) tmpMin = 0.0;
+    if (tmpMax > 2 * pi) tmpMax = 2 * pi;
+    if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
+    *mx = tmpMax;
+    *mn = tmpMin;
+    return bad;
+}
+
 int or_extrema(int n_dihedrals, int n_frames, double *bonds, double *angles, double *dihedrals,
                double *min_b, double *max_b, double *min_a, double *max_a,
                double *min_d, double *max_d, double *modfit) {
@@ -84,97 +195,12 @@ int or_extrema(int n_dihedrals, int n_frames, double *bonds, double *angles, dou
     const size_t F = (size_t)n_frames;
     int bad = 0;
 #pragma omp parallel for reduction(+ : bad) schedule(dynamic)
-    for (int j = 0; j < nb; j++) { /* PARENT.cpp:511-536 */
-        const double *x = bonds + j * F;
-        double tmpMax = -1.0e100, tmpMin = 1.0e100;
-        for (size_t i = 0; i < F; i++) {
-            if (x[i] > tmpMax) tmpMax = x[i];
-            if (x[i] < tmpMin) tmpMin = x[i];
-        }
-        if ((tmpMin < 0.0) || (tmpMax < 0.0)) bad++;
-        tmpMin -= 0.000000005;
-        tmpMax += 0.000000005;
-        if (tmpMin < 0.0) tmpMin = 0.0;
-        if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
-        max_b[j] = tmpMax;
-        min_b[j] = tmpMin;
-    }
+    for (int j = 0; j < nb; j++) bad += ext_bond(bonds + j * F, F, &min_b[j], &max_b[j]);
 #pragma omp parallel for schedule(dynamic)
-    for (int j = 0; j < na; j++) { /* PARENT.cpp:538-562 */
-        const double *x = angles + j * F;
-        double tmpMax = -1.0e100, tmpMin = 1.0e100;
-        for (size_t i = 0; i < F; i++) {
-            if (x[i] > tmpMax) tmpMax = x[i];
-            if (x[i] < tmpMin) tmpMin = x[i];
-        }
-        tmpMin -= 0.000000005;
-        tmpMax += 0.000000005;
-        if (tmpMin < 0) tmpMin = 0;
-        if (tmpMax > pi) tmpMax = pi;
-        if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
-        max_a[j] = tmpMax;
-        min_a[j] = tmpMin;
-    }
+    for (int j = 0; j < na; j++) ext_angle(angles + j * F, F, pi, &min_a[j], &max_a[j]);
 #pragma omp parallel for reduction(+ : bad) schedule(dynamic)
-    for (int j = 0; j < nd; j++) { /* PARENT.cpp:564-637 */
-        double *x = dihedrals + j * F;
-        long long histo[MODFITNBINS];
-        for (int k = 0; k < MODFITNBINS; k++) histo[k] = 0;
-        const double binsize = (2 * pi + 0.000000005) / MODFITNBINS;
-        for (size_t i = 0; i < F; i++) {
-            int idx = (int)((x[i]) / binsize);
-            if (idx < 0 || idx >= MODFITNBINS) { bad++; idx = idx < 0 ? 0 : MODFITNBINS - 1; }
-            histo[idx] += 1;
-        }
-        int zeroExists = 0;
-        for (int k = 0; k < MODFITNBINS; k++) zeroExists = zeroExists || (histo[k] == 0);
-        int longestZeroStretch, longestZeroStretchPos, currentZeroStretch, currentZeroStretchPos = 0;
-        if (zeroExists) {
-            longestZeroStretch = 0;
-            currentZeroStretch = 0;
-            longestZeroStretchPos = -1;
-            for (int k = 0; k < 2 * MODFITNBINS; k++) {
-                int l = k % MODFITNBINS;
-                if ((currentZeroStretch == 0) && (histo[l] == 0)) {
-                    currentZeroStretch = 1;
-                    currentZeroStretchPos = k;
-                }
-                if ((currentZeroStretch > 0) && (histo[l] == 0)) currentZeroStretch += 1;
-                if ((currentZeroStretch > 0) && (histo[l] != 0)) {
-                    if (currentZeroStretch > longestZeroStretch) {
-                        longestZeroStretch = currentZeroStretch;
-                        longestZeroStretchPos = currentZeroStretchPos;
-                    }
-                    currentZeroStretch = 0;
-                }
-            }
-        } else {
-            longestZeroStretchPos = 0;
-            longestZeroStretch = (int)histo[0];
-            for (int k = 0; k < MODFITNBINS; k++) {
-                if (histo[k] < longestZeroStretch) {
-                    longestZeroStretch = (int)histo[k];
-                    longestZeroStretchPos = k;
-                }
-            }
-        }
-        const double modFit = 2 * pi - (longestZeroStretchPos + 0.5) * binsize;
-        if (modfit) modfit[j] = modFit;
-        for (size_t k = 0; k < F; k++)
-            x[k] = x[k] + modFit - 2 * pi * (int)((x[k] + modFit) / (2 * pi));
-        double tmpMax = -1.0e100, tmpMin = 1.0e100;
-        for (size_t i = 0; i < F; i++) {
-            if (x[i] > tmpMax) tmpMax = x[i];
-            if (x[i] < tmpMin) tmpMin = x[i];
-        }
-        tmpMin -= 0.000000005;
-        tmpMax += 0.000000005;
-        if (tmpMin < 0.0) tmpMin = 0.0;
-        if (tmpMax > 2 * pi) tmpMax = 2 * pi;
-        if ((tmpMax - tmpMin) < 1.0e-4) tmpMax += 0.05;
-        max_d[j] = tmpMax;
-        min_d[j] = tmpMin;
-    }
+    for (int j = 0; j < nd; j++)
+        bad += ext_dih(dihedrals + j * F, F, pi, &min_d[j], &max_d[j], modfit ? &modfit[j] : NULL);
     return bad;
 }
 
@@ -366,6 +392,73 @@ int or_parent(int n_dihedrals, int n_frames, double *bonds, double *angles, doub
     return bad ? 2 : 0;
 }
 
+/* ------------------------------------------------ sampled full-size check */
+
+/* Column j (global DOF index) as FP64, promoted from FP32 exactly as
+ * read_BAT_frame does (io_binary.cpp:322-364). */
+static void load_col(int prec, const void *base, long long ld, int j, size_t F, double *out) {
+    if (prec) {
+        const double *x = (const double *)base + (size_t)j * (size_t)ld;
+        memcpy(out, x, sizeof(double) * F);
+    } else {
+        const float *x = (const float *)base + (size_t)j * (size_t)ld;
+        for (size_t i = 0; i < F; i++) out[i] = x[i];
+    }
+}
+
+int or_sample(int n_dihedrals, int n_frames, int double_prec, const void *bonds, const void *angles,
+              const void *dihedrals, long long ld, const int bins[6], int n_pairs, const int *g1,
+              const int *g2, double *s1, double *s2, int n_counts, int64_t *counts, long long count_stride,
+              double *mn, double *mx, double *modfit) {
+    const double pi = acos(-1); /* PARENT.cpp:112 */
+    const int nb = n_dihedrals + 2, na = n_dihedrals + 1, D = nb + na + n_dihedrals;
+    const size_t F = (size_t)n_frames;
+    for (int k = 0; k < 6; k++)
+        if (bins[k] < 1) return 1;
+    const void *src[3] = {bonds, angles, dihedrals};
+    const int lo[3] = {0, nb, nb + na};
+    int bad = 0;
+    /* per DOF: extrema (and the dihedral shift) and the 1D entropy */
+#pragma omp parallel reduction(+ : bad)
+    {
+        double *x = malloc(sizeof(double) * (F ? F : 1));
+#pragma omp for schedule(dynamic, 4)
+        for (int g = 0; g < D; g++) {
+            const int t = g < nb ? 0 : (g < nb + na ? 1 : 2);
+            load_col(double_prec, src[t], ld, g - lo[t], F, x);
+            modfit[g] = 0.0;
+            if (t == 0) bad += ext_bond(x, F, &mn[g], &mx[g]);
+            else if (t == 1) ext_angle(x, F, pi, &mn[g], &mx[g]);
+            else bad += ext_dih(x, F, pi, &mn[g], &mx[g], &modfit[g]);
+            s1[g] = or_entropy1d(t, x, n_frames, mn[g], mx[g], bins[t], &bad);
+        }
+        free(x);
+    }
+    /* per pair: both columns (shifted as above), the 2D entropy */
+#pragma omp parallel reduction(+ : bad)
+    {
+        double *x = malloc(sizeof(double) * (F ? F : 1));
+        double *y = malloc(sizeof(double) * (F ? F : 1));
+#pragma omp for schedule(dynamic, 1)
+        for (int k = 0; k < n_pairs; k++) {
+            const int a = g1[k], b = g2[k];
+            if (a < 0 || b >= D || a >= b) { s2[k] = NAN; bad++; continue; }
+            const int ta = a < nb ? 0 : (a < nb + na ? 1 : 2), tb = b < nb ? 0 : (b < nb + na ? 1 : 2);
+            load_col(double_prec, src[ta], ld, a - lo[ta], F, x);
+            load_col(double_prec, src[tb], ld, b - lo[tb], F, y);
+            if (ta == 2)
+                for (size_t i = 0; i < F; i++) x[i] = dih_shift(x[i], modfit[a], pi);
+            if (tb == 2)
+                for (size_t i = 0; i < F; i++) y[i] = dih_shift(y[i], modfit[b], pi);
+            s2[k] = or_entropy2d(ta, x, mn[a], mx[a], bins[3 + ta], tb, y, mn[b], mx[b], bins[3 + tb], n_frames,
+                                 k < n_counts ? counts + (size_t)k * (size_t)count_stride : NULL, &bad);
+        }
+        free(x);
+        free(y);
+    }
+    return bad ? 2 : 0;
+}
+
 /* ---------------------------------------------------------------- MI / MIE */
 
 double or_mutual(int type, int index1, int index2, int n_dihedrals,
@@ -441,33 +534,38 @@ void or_mie_totals(int n_dihedrals, const double *s1_b, const double *s1_a, cons
 
 /* ---------------------------------------------------------------- MIST */
 
-void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const double *s1_d,
-             const double *bb, const double *ba, const double *bd,
-             const double *aa, const double *ad, const double *dd,
-             int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
-             int *edge_left, double totals[10]) {
+/* The step's first maximum of one thread's contiguous range of the scan
+ * sequence, and the largest value elsewhere in that range. */
+typedef struct {
+    double best, second;
+    long long at; /* position in the step's scan sequence, -1 if none */
+} scan_best;
+
+void or_mist_gap(int n_dihedrals, const double *s1_b, const double *s1_a, const double *s1_d,
+                 const double *bb, const double *ba, const double *bd,
+                 const double *aa, const double *ad, const double *dd,
+                 int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
+                 int *edge_left, double *edge_gap, double totals[10]) {
     const int nb = n_dihedrals + 2, na = n_dihedrals + 1, nd = n_dihedrals;
-    const int cnt[3] = {nb, na, nd};
-    /* dense matrices, get_PAR_MIST.cpp:290-327: mutual[BB|AA|DD] symmetric,
-     * mutual[BA] nb x na, mutual[BD] nb x nd, mutual[AD] na x nd */
-    double *M[6];
-    const int r[6] = {nb, nb, nb, na, na, nd}, c[6] = {nb, na, nd, na, nd, nd};
-    for (int q = 0; q < 6; q++) M[q] = calloc((size_t)r[q] * c[q] + 1, sizeof(double));
-    for (int i = 0; i < nb - 1; i++)
-        for (int j = i + 1; j < nb; j++)
-            M[0][(size_t)i * nb + j] = M[0][(size_t)j * nb + i] = or_mutual(0, i, j, MARGS);
-    for (int i = 0; i < nb; i++)
-        for (int j = 0; j < na; j++) M[1][(size_t)i * na + j] = or_mutual(1, i, j, MARGS);
-    for (int i = 0; i < nb; i++)
-        for (int j = 0; j < nd; j++) M[2][(size_t)i * nd + j] = or_mutual(2, i, j, MARGS);
-    for (int i = 0; i < na - 1; i++)
-        for (int j = i + 1; j < na; j++)
-            M[3][(size_t)i * na + j] = M[3][(size_t)j * na + i] = or_mutual(3, i, j, MARGS);
-    for (int i = 0; i < na; i++)
-        for (int j = 0; j < nd; j++) M[4][(size_t)i * nd + j] = or_mutual(4, i, j, MARGS);
-    for (int i = 0; i < nd - 1; i++)
-        for (int j = i + 1; j < nd; j++)
-            M[5][(size_t)i * nd + j] = M[5][(size_t)j * nd + i] = or_mutual(5, i, j, MARGS);
+    const int cnt[3] = {nb, na, nd}, lo[3] = {0, nb, nb + na};
+    const int D = nb + na + nd;
+    /* the six matrices of get_PAR_MIST.cpp:290-327 (get_mutual values, bb/aa/dd
+     * symmetrised) held as one symmetric D x D matrix over global DOF indices:
+     * the scan below reads mutual[type(u)type(v)][u][v] as M[u][v] */
+    double *M = calloc((size_t)D * D + 1, sizeof(double));
+    const int t1s[6] = {0, 0, 0, 1, 1, 2}, t2s[6] = {0, 1, 2, 1, 2, 2};
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int i = 0; i < D; i++) {
+        const int ti = i < nb ? 0 : (i < nb + na ? 1 : 2);
+        for (int j = i + 1; j < D; j++) {
+            const int tj = j < nb ? 0 : (j < nb + na ? 1 : 2);
+            int q = 0;
+            while (!(t1s[q] == ti && t2s[q] == tj)) q++;
+            const double v = or_mutual(q, i - lo[ti], j - lo[tj], MARGS);
+            M[(size_t)i * D + j] = v;
+            M[(size_t)j * D + i] = v;
+        }
+    }
 
     double tB = 0, tA = 0, tD = 0;
     for (int k = 0; k < nb; k++) tB += s1_b[k];
@@ -487,26 +585,86 @@ void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const doub
     nOut[0]--;
 
     double tm = 0, tpair[6] = {0};
-    /* block order BB BA BD AB AA AD DB DA DD, get_PAR_MIST.cpp:481-606 */
     int step = 0;
+    int maxthr = 1;
+#ifdef _OPENMP
+    maxthr = omp_get_max_threads();
+#endif
+    scan_best *part = malloc(sizeof(scan_best) * (size_t)maxthr);
     while (nOut[0] + nOut[1] + nOut[2] > 0) {
-        double best = -1e200;
-        int bt1 = 0, bt2 = 0, bi = 0, bj = 0;
-        for (int ti = 0; ti < 3; ti++)
-            for (int to = 0; to < 3; to++)
-                for (int i = 0; i < nIn[ti]; i++)
-                    for (int j = 0; j < nOut[to]; j++) {
-                        int u = In[ti][i], v = Out[to][j];
-                        double val;
-                        if (ti <= to) {
-                            int q = ti == 0 ? to : (ti == 1 ? 2 + to : 5);
-                            val = M[q][(size_t)u * c[q] + v];
-                        } else {
-                            int q = to == 0 ? ti : 4; /* (1,0)->BA, (2,0)->BD, (2,1)->AD */
-                            val = M[q][(size_t)v * c[q] + u];
+        /* The step's scan sequence, get_PAR_MIST.cpp:481-606: blocks (In type,
+         * Out type) in the order BB BA BD AB AA AD DB DA DD, within a block In
+         * position i then Out position j; the FIRST strict maximum wins. The
+         * sequence is cut into one contiguous range per thread; merging the
+         * ranges in order with the same strict '>' gives the serial result. */
+        long long bsz[9], bstart[10];
+        bstart[0] = 0;
+        for (int b = 0; b < 9; b++) {
+            bsz[b] = (long long)nIn[b / 3] * nOut[b % 3];
+            bstart[b + 1] = bstart[b] + bsz[b];
+        }
+        const long long W = bstart[9];
+        int nthr = 1;
+#pragma omp parallel num_threads(maxthr)
+        {
+            const int t = omp_thread();
+            const int nthr_here = omp_nthreads();
+#pragma omp single
+            nthr = nthr_here;
+            /* the single's implied barrier: every thread sees the team size */
+            const long long p0 = W * t / nthr_here, p1 = W * (t + 1) / nthr_here;
+            scan_best r = {-1e200, -INFINITY, -1};
+            long long pos = p0;
+            int b = 0;
+            while (b < 9 && bstart[b + 1] <= pos) b++;
+            while (pos < p1 && b < 9) {
+                if (bsz[b] == 0) { b++; continue; }
+                const int ti = b / 3, to = b % 3, no = nOut[to];
+                const long long off = pos - bstart[b];
+                int i = (int)(off / no), j = (int)(off % no);
+                const long long bend = bstart[b + 1] < p1 ? bstart[b + 1] : p1;
+                for (; pos < bend; i++, j = 0) {
+                    const double *row = M + (size_t)(lo[ti] + In[ti][i]) * D + lo[to];
+                    const int *o = Out[to];
+                    const int jend = (int)((bend - pos) < (no - j) ? j + (bend - pos) : no);
+                    for (int jj = j; jj < jend; jj++) {
+                        const double val = row[o[jj]];
+                        if (val > r.best) {
+                            if (r.at >= 0 && r.best > r.second) r.second = r.best;
+                            r.best = val;
+                            r.at = pos + (jj - j);
+                        } else if (val > r.second) {
+                            r.second = val;
                         }
-                        if (val > best) { best = val; bt1 = ti; bt2 = to; bi = i; bj = j; }
                     }
+                    pos += jend - j;
+                }
+                b++;
+            }
+            part[t] = r;
+        }
+        scan_best g = {-1e200, -INFINITY, -1};
+        for (int t = 0; t < nthr; t++) {
+            const scan_best r = part[t];
+            if (r.at >= 0 && r.best > g.best) {
+                if (g.at >= 0 && g.best > g.second) g.second = g.best;
+                g.best = r.best;
+                g.at = r.at;
+            } else if (r.at >= 0 && r.best > g.second) {
+                g.second = r.best;
+            }
+            if (r.second > g.second) g.second = r.second;
+        }
+        int bt1 = 0, bt2 = 0, bi = 0, bj = 0;
+        double best = g.best;
+        if (g.at >= 0) {
+            int b = 0;
+            while (bstart[b + 1] <= g.at) b++;
+            bt1 = b / 3;
+            bt2 = b % 3;
+            bi = (int)((g.at - bstart[b]) / nOut[bt2]);
+            bj = (int)((g.at - bstart[b]) % nOut[bt2]);
+        }
         tm += best;
         edge_t1[step] = bt1;
         edge_t2[step] = bt2;
@@ -514,19 +672,29 @@ void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const doub
         edge_i2[step] = Out[bt2][bj] + 1;
         edge_mi[step] = best;
         edge_left[step] = nOut[0] + nOut[1] + nOut[2];
+        if (edge_gap) edge_gap[step] = W > 1 ? best - g.second : INFINITY;
         In[bt2][nIn[bt2]++] = Out[bt2][bj];
         memmove(Out[bt2] + bj, Out[bt2] + bj + 1, sizeof(int) * (nOut[bt2] - bj - 1));
         nOut[bt2]--;
-        const int lo = bt1 < bt2 ? bt1 : bt2, hi = bt1 < bt2 ? bt2 : bt1;
-        const int q = lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+        const int lo2 = bt1 < bt2 ? bt1 : bt2, hi2 = bt1 < bt2 ? bt2 : bt1;
+        const int q = lo2 == 0 ? hi2 : (lo2 == 1 ? 2 + hi2 : 5);
         tpair[q] += best;
         step++;
     }
+    free(part);
     totals[0] = tB; totals[1] = tA; totals[2] = tD;
     for (int q = 0; q < 6; q++) totals[3 + q] = tpair[q];
     totals[9] = tB + tA + tD - tm;
     for (int t = 0; t < 3; t++) { free(In[t]); free(Out[t]); }
-    for (int q = 0; q < 6; q++) free(M[q]);
+    free(M);
+}
+
+void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const double *s1_d,
+             const double *bb, const double *ba, const double *bd,
+             const double *aa, const double *ad, const double *dd,
+             int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
+             int *edge_left, double totals[10]) {
+    or_mist_gap(MARGS, edge_t1, edge_t2, edge_i1, edge_i2, edge_mi, edge_left, NULL, totals);
 }
 
 /* ------------------------------------------------------- BAT conversion */

@@ -81,6 +81,31 @@ void or_mist(int n_dihedrals, const double *s1_b, const double *s1_a, const doub
              int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
              int *edge_left, double totals[10]);
 
+/* or_mist plus, per step, the gap between the winning MI and the largest
+ * other candidate value of that step's scan (0 where the winner was decided
+ * by the scan order among equal values; INFINITY for a single candidate).
+ * The scan runs on all OpenMP threads over contiguous ranges of the step's
+ * scan sequence, merged in order: the result is the serial scan's. */
+void or_mist_gap(int n_dihedrals, const double *s1_b, const double *s1_a, const double *s1_d,
+                 const double *bb, const double *ba, const double *bd,
+                 const double *aa, const double *ad, const double *dd,
+                 int *edge_t1, int *edge_t2, int *edge_i1, int *edge_i2, double *edge_mi,
+                 int *edge_left, double *edge_gap, double totals[10]);
+
+/* Full-size parity on a sample: for every DOF (global index, bonds | angles |
+ * dihedrals) the extrema and dihedral shift of PARENT.cpp:504-638 and the 1D
+ * entropy at bins[0..2] (s1[D], mn[D], mx[D], modfit[D], 0 for non-dihedrals);
+ * for each listed pair g1[k] < g2[k] the 2D entropy of PARENT.cpp:786-1479
+ * (s2[k]) and, for k < n_counts, its B1 x B2 counts at counts + k*count_stride.
+ * Columns are FP32 (double_prec 0, promoted as read_BAT_frame does) or FP64,
+ * DOF-major with leading dimension ld, per type; they are not modified and
+ * no FP64 copy of the whole trajectory is made. Returns 0, or nonzero if a
+ * bond was negative or an index left its range. */
+int or_sample(int n_dihedrals, int n_frames, int double_prec, const void *bonds, const void *angles,
+              const void *dihedrals, long long ld, const int bins[6], int n_pairs, const int *g1,
+              const int *g2, double *s1, double *s2, int n_counts, int64_t *counts, long long count_stride,
+              double *mn, double *mx, double *modfit);
+
 /* Cartesian -> BAT columns as BAT_builder converts a trajectory frame by
  * frame (BAT_trajectory.cpp:114-125): coordinates scaled by 10 (nm ->
  * Angstrom, stored back as float), convert_to_BAT (:219-300),

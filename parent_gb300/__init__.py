@@ -353,11 +353,11 @@ class Engine:
         _check(lib().pg_entropy_shard(self._ctx, C.byref(v), b, f, shard, n_shards, C.byref(body)), self._ctx)
         return out
 
-    def pair_counts(self, traj: Trajectory, bins, pairs, form: str = "hist") -> list[np.ndarray]:
+    def pair_counts(self, traj: Trajectory | BatView, bins, pairs, form: str = "hist") -> list[np.ndarray]:
         """Raw 2D histograms of explicit (g1 < g2) pairs from the GPU pair kernel."""
-        v = traj.view()
+        v = traj if isinstance(traj, BatView) else traj.view()
         b = (C.c_int * 6)(*bins)
-        nb, na = traj.n_dih + 2, traj.n_dih + 1
+        nb, na = v.n_dihedrals + 2, v.n_dihedrals + 1
         tb = lambda g: 0 if g < nb else (1 if g < nb + na else 2)
         g1 = (C.c_int * len(pairs))(*[p[0] for p in pairs])
         g2 = (C.c_int * len(pairs))(*[p[1] for p in pairs])

@@ -126,9 +126,11 @@ def build_oracle() -> Path:
     against."""
     oracle = ROOT / "oracle"
     _run(["make", "-s", "-C", str(oracle)])
-    ref_root = os.environ.get("PG_REFERENCE_ROOT", "/root/reference")
-    if (Path(ref_root) / "src" / "PARENT" / "PARENT.cpp").exists():
-        _run(["make", "-s", "-C", str(oracle), "ref", f"REF_ROOT={ref_root}", "-j4"])
+    # the recipe's REF_ROOT (or PG_REFERENCE_ROOT) says where the reference sources are
+    r = subprocess.run(["make", "-s", "-C", str(oracle), "print-ref-root"], capture_output=True, text=True)
+    ref_root = r.stdout.strip()
+    if ref_root and (Path(ref_root) / "src" / "PARENT" / "PARENT.cpp").exists():
+        _run(["make", "-s", "-C", str(oracle), "ref", "-j4"])
     return oracle / "liboracle.so"
 
 

@@ -267,7 +267,7 @@ mist_cluster_kernel(int D, int nb, int na, const double *__restrict__ mi, double
             edge_to[step] = b.v;
         }
         if (b.v >= 0 && w >= v0 && w < v0 + nloc && (w - v0) % nthr == tid) from[w - v0] = -2;  // its owner
-        if (tid == 0) pos[w] = step + 1;  // read from step + 2 on, after the next barrier
+        if (b.v >= 0 && tid == 0) pos[w] = step + 1;  // read from step + 2 on, after the next barrier
         last_w = w;
         last_pos = step + 1;
     }

@@ -13,8 +13,6 @@
 // DOF). Here it lives in a file-scope __device__ array sized for
 // PG_NOALLOC_MAX_DOFS DOFs, which every GPU that loads the library keeps
 // until the process exits.
-#include <mutex>
-
 #include "../../include/parent_gb300.h"
 #include "pg_internal.h"
 
@@ -32,36 +30,20 @@ namespace {
 constexpr size_t kScratchBytes = (size_t)PG_NOALLOC_MAX_DOFS * 16 + 256;
 __device__ __align__(256) unsigned char g_mist_scratch[kScratchBytes];
 
-// Device address of g_mist_scratch per device. In host code the array's name
-// is only a host-side stand-in, so the address is looked up once per device
-// with that device current.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
-
+// Device address of g_mist_scratch on the current device. In host code the
+// array's name is only a host-side stand-in, so the address is looked up
+// with the device current. The lookup is repeated on every call (it is cheap
+// and enqueues nothing): a cached address would dangle after the host program
+// resets the device, which reloads the module.
 int scratch_for_current_device(void **out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        pg::set_global_error(cudaGetErrorString(e));
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_mist_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();  // leave no error of this lookup behind
+        pg::set_global_error(e != cudaSuccess ? cudaGetErrorString(e) : "pg_mist_noalloc: null scratch address");
         return PG_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        pg::set_global_error("pg_mist_noalloc: device index beyond the supported 64");
-        return PG_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_mist_scratch);
-        if (e != cudaSuccess || !p) {
-            pg::set_global_error(e != cudaSuccess ? cudaGetErrorString(e)
-                                                  : "pg_mist_noalloc: null scratch address");
-            return PG_ERR_CUDA;
-        }
-        g_addr[dev] = p;
-    }
-    *out = g_addr[dev];
+    *out = p;
     return PG_OK;
 }
 
@@ -87,12 +69,18 @@ extern "C" PG_API int pg_mist_noalloc(int n_dihedrals, const double *mi, double 
         pg::set_global_error("pg_mist_noalloc: scratch layout larger than the static array");
         return PG_ERR_UNSUPPORTED;
     }
+    // an error left by the host program's own earlier CUDA calls on this
+    // thread is not this call's
+    cudaGetLastError();
     void *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != PG_OK) return rc;
-    // the kernel initialises every key/from entry it reads and writes each
-    // insertion position before reading it, so leftover contents of the
-    // shared array from an earlier call need no clearing
+    // Only the one-CTA kernel on more DOFs than its shared memory holds
+    // (above 12,800 DOFs, with the cluster kernel switched off by
+    // PG_MIST_CLUSTER=0) keeps its per-DOF arrays in this static array; the
+    // other kernels keep them in shared memory. That kernel initialises every
+    // key/from entry it reads and writes each insertion position before
+    // reading it, so leftover contents of an earlier call need no clearing.
     const int nb = n_dihedrals + 2, na = n_dihedrals + 1;
     cudaError_t e = pg::launch_mist_impl((int)D, nb, na, mi, scratch, edge_mi, edge_from, edge_to,
                                          (cudaStream_t)stream);

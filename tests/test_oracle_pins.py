@@ -14,7 +14,7 @@ import pytest
 import oracle
 from conftest import FIXTURES, GOLDEN, par_body_from_file, read_text_gz
 
-REF_ROOT = Path(os.environ.get("PG_REFERENCE_ROOT", "/root/reference"))
+REF_ROOT = oracle.reference_root()
 
 TOTAL_NAMES_MIST = ["TOTAL 1D BONDS ENTROPY", "TOTAL 1D ANGLES ENTROPY", "TOTAL 1D DIHEDRALS ENTROPY",
                     "TOTAL 2D BONDS-BONDS MUTUAL INFORMATION", "TOTAL 2D BONDS-ANGLES MUTUAL INFORMATION",

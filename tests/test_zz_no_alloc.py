@@ -3,10 +3,14 @@
 Callers that own the whole device memory budget (a pre-allocated pool in the
 host program) or that cannot accept an allocation's device-wide
 synchronisation pass their own device buffers for the MI matrix and the edge
-list; the kernel's scratch is a static device array inside the library. This
-test calls it through the C ABI twice in a row on different systems and
-checks each result against pg_mist, the allocating entry point, plus the
-size rejection. It sits in its own file so that pytest collects it last.
+list; the kernel's scratch is a static device array inside the library. These
+tests call it through the C ABI twice in a row and check each result against
+pg_mist, the allocating entry point: on the two golden fixtures (the one-CTA
+kernel with shared-memory arrays), on 1,194 DOFs (the cluster kernel, also
+against the oracle), and on 16,383 then 12,903 DOFs with the cluster kernel
+off, the only path whose per-DOF arrays live in the static array (the second
+call starts on the first one's leftovers). Plus the size rejection. It sits in
+its own file so that pytest collects it last.
 """
 from __future__ import annotations
 
@@ -98,6 +102,60 @@ def test_noalloc_matches_pg_mist_on_two_calls():
             assert np.array_equal(t1, ref["t1"]) and np.array_equal(t2, ref["t2"])
             assert np.array_equal(i1, ref["i1"]) and np.array_equal(i2, ref["i2"])
             assert np.max(np.abs(mi - ref["mi"])) <= 1e-9
+
+
+def dyadic_body(n: int, seed: int) -> pg.ParBody:
+    """A random .par body on a grid of 1/64: sums of its values are exact, so
+    many MI terms tie exactly and the reference's scan order decides."""
+    rng = np.random.default_rng(seed)
+    body = pg.ParBody.empty(n)
+    for k, v in body.blocks.items():
+        mu = 1.0 if k.startswith("s1") else 1.5
+        v[:] = np.round(rng.normal(mu, 0.25, v.size) * 64.0) / 64.0
+    return body
+
+
+def check_against(eng, n, body, edges_fn):
+    ref, _ = eng.mist(n, body)
+    t1, t2, i1, i2, mi = edges_fn()
+    assert np.array_equal(t1, ref["t1"]) and np.array_equal(t2, ref["t2"])
+    assert np.array_equal(i1, ref["i1"]) and np.array_equal(i2, ref["i2"])
+    assert np.array_equal(mi, ref["mi"])
+    return ref
+
+
+def test_noalloc_cluster_kernel_matches_pg_mist_and_the_oracle():
+    # from 1,024 DOFs the eight-CTA cluster kernel runs (per-DOF arrays in
+    # shared memory); 1,194 DOFs with many exact ties
+    import oracle
+    n = 397
+    body = dyadic_body(n, 11)
+    with pg.Engine(0) as eng:
+        M = dense_mi(n, body)
+        for _ in range(2):
+            ref = check_against(eng, n, body, lambda: as_edges(n, *run_noalloc(eng, n, M)))
+    oe, _ = oracle.mist(n, body.blocks)
+    for f in ("t1", "t2", "i1", "i2"):
+        assert np.array_equal(oe[f], ref[f]), f
+
+
+def test_noalloc_static_array_path_on_two_calls(monkeypatch):
+    # one CTA with the cluster kernel off: above 12,800 DOFs its per-DOF arrays
+    # leave shared memory for the static array. Two calls in a row, the larger
+    # first, so the second starts on the first one's leftover contents; each
+    # equals pg_mist with the same setting (the same kernel on allocated
+    # scratch) and pg_mist with the cluster kernel (another kernel, checked
+    # against the oracle elsewhere).
+    with pg.Engine(0) as eng:
+        for n, seed in ((5460, 21), (4300, 22)):       # D = 16,383 and 12,903
+            body = dyadic_body(n, seed)
+            M = dense_mi(n, body)
+            monkeypatch.setenv("PG_MIST_CLUSTER", "0")
+            got = as_edges(n, *run_noalloc(eng, n, M))
+            check_against(eng, n, body, lambda: got)
+            monkeypatch.delenv("PG_MIST_CLUSTER")
+            check_against(eng, n, body, lambda: got)
+            del M
 
 
 def test_noalloc_rejects_sizes_beyond_its_maximum():
