@@ -184,9 +184,11 @@ static DofArrays dof_arrays(pg_ctx *ctx, int D) {
 static size_t elem_size(int prec) { return prec ? 8 : 4; }
 
 // Validation and the geometry of a trajectory (ctx->geo).
-static bool needs_row_codes(const SysGeom &g);
+static void set_bin_layout(SysGeom &g, int form);
 
-static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
+// form: the form the caller asked for (PG_FORM_AUTO/HIST/ONEHOT); it decides
+// the bin-matrix layout the preprocessing writes (set_bin_layout).
+static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int form) {
     if (!tv || !bins) return fail(ctx, PG_ERR_ARG, "null trajectory or bins");
     if (tv->n_dihedrals < 0 || tv->n_frames < 1)
         return fail(ctx, PG_ERR_ARG, "n_dihedrals (%d) < 0 or n_frames (%d) < 1", tv->n_dihedrals, tv->n_frames);
@@ -211,16 +213,15 @@ static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6])
     g.F = tv->n_frames;
     g.ldb = bins_ld(g.F);
     for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
-    g.codes = 0;
-    g.codes = needs_row_codes(g) ? 1 : 0;
+    set_bin_layout(g, form);
     ctx->resident = false;
     return PG_OK;
 }
 
 // Shared front half of pg_entropy / pg_pair_counts: validation, upload,
 // preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
-static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6]) {
-    int rc0 = setup_geometry(ctx, tv, bins);
+static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int form) {
+    int rc0 = setup_geometry(ctx, tv, bins, form);
     if (rc0) return rc0;
     const SysGeom &g = ctx->geo;
     const int D = g.D;
@@ -324,20 +325,39 @@ static int ensure_fix_table(pg_ctx *ctx, int F) {
     return PG_OK;
 }
 
-// Histogram layout, from measured inner-loop rates: the 32-slot kernel with
-// 32-bit counters (one wavefront per warp-wide reduction) for 2D bin counts
-// up to 35; the 16-slot kernel (two lanes per pair) above that, where the
-// 32-slot kernel needs 16-bit counters. PG_HIST_SLOTS=16 or 32 forces one
-// layout (32 slots up to 50 bins).
-static bool use_hist32(const SysGeom &g) {
-    const char *e = getenv("PG_HIST_SLOTS");
-    if (e && atoi(e) == 16) return false;
-    if (e && atoi(e) == 32) return pairs_hist32_supported(bmax_of(g));
-    return pairs_hist32_wide(bmax_of(g));
-}
+// Histogram layouts: the 16-slot kernel (two lanes per pair), the 32-slot
+// kernel fed by a TMA ring, and the streamed 32-slot kernel (rows loaded
+// straight from the frame-group interleaved bin matrix).
+enum { HIST16 = 0, HIST32_RING = 1, HIST32_STREAM = 2 };
 
-// The 16-bit 32-slot layout stages its row DOFs from the row-code matrix.
-static bool needs_row_codes(const SysGeom &g) { return use_hist32(g) && !pairs_hist32_wide(bmax_of(g)); }
+// From measured inner-loop rates: the 32-slot ring kernel with 32-bit
+// counters (one wavefront per warp-wide reduction) for 2D bin counts up to
+// 35; the 16-slot kernel above that, where the 32-slot kernels need 16-bit
+// counters. PG_HIST_SLOTS=16 or 32 forces the 16-slot or the 32-slot ring
+// layout (32 slots up to 50 bins); PG_HIST_STREAM=1 the streamed one.
+static int hist_layout(const SysGeom &g) {
+    const int bm = bmax_of(g);
+    const char *e = getenv("PG_HIST_SLOTS");
+    const char *st = getenv("PG_HIST_STREAM");
+    if (e && atoi(e) == 16) return HIST16;
+    if (st && atoi(st) == 1 && pairs_hist32_supported(bm)) return HIST32_STREAM;
+    if (e && atoi(e) == 32) return pairs_hist32_supported(bm) ? HIST32_RING : HIST16;
+    return pairs_hist32_wide(bm) ? HIST32_RING : HIST16;
+}
+static bool use_hist32(const SysGeom &g) { return hist_layout(g) != HIST16; }
+
+// The bin matrices the preprocessing writes for a form: the 16-bit 32-slot
+// layouts stage their row DOFs from the row-code matrix; the streamed layout
+// reads both matrices frame-group interleaved; the one-hot form and the
+// 16-slot kernel read plain DOF rows.
+static void set_bin_layout(SysGeom &g, int form) {
+    int chosen = form == PG_FORM_AUTO ? autotune_form(g) : form;
+    if (chosen == PG_FORM_ONEHOT && !pairs_onehot_supported(g)) chosen = PG_FORM_HIST;
+    const bool hist = chosen != PG_FORM_ONEHOT;
+    const int layout = hist ? hist_layout(g) : HIST16;
+    g.codes = layout != HIST16 && !pairs_hist32_wide(bmax_of(g)) ? 1 : 0;
+    g.ilv = layout == HIST32_STREAM ? 1 : 0;
+}
 
 // Launches the 32-slot kernel over the cached full tile list (explicit ==
 // nullptr) or over n_explicit given tiles; the per-CTA accumulators live in
@@ -847,12 +867,12 @@ PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], i
     cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (form < PG_FORM_AUTO || form > PG_FORM_ONEHOT) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
     if (traj && !traj->on_device && form != PG_FORM_ONEHOT) {
-        int rc0 = setup_geometry(ctx, traj, bins);
+        int rc0 = setup_geometry(ctx, traj, bins, form);
         if (rc0) return rc0;
         const int f = form == PG_FORM_AUTO ? autotune_form(ctx->geo) : form;
         if (f != PG_FORM_ONEHOT || !pairs_onehot_supported(ctx->geo)) return run_streamed(ctx, traj, out);
     }
-    int rc = run_prep(ctx, traj, bins);
+    int rc = run_prep(ctx, traj, bins, form);
     if (rc) return rc;
     const SysGeom &g = ctx->geo;
     cudaStream_t st = ctx->stream;
@@ -968,7 +988,7 @@ PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins
     if (n_shards < 1 || shard < 0 || shard >= n_shards) return fail(ctx, PG_ERR_ARG, "shard %d of %d", shard, n_shards);
     if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "shards use the histogram form");
     if (form != PG_FORM_AUTO && form != PG_FORM_HIST) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
-    int rc = run_prep(ctx, traj, bins);  // every shard bins all D columns (O(D F))
+    int rc = run_prep(ctx, traj, bins, PG_FORM_HIST);  // every shard bins all D columns (O(D F))
     if (rc) return rc;
     const SysGeom &g = ctx->geo;
     cudaStream_t st = ctx->stream;
@@ -1027,7 +1047,7 @@ PG_API int pg_pair_counts(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6
     cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (n_pairs < 0 || (n_pairs > 0 && (!g1 || !g2 || !counts))) return fail(ctx, PG_ERR_ARG, "bad pair list");
     if (form == PG_FORM_ONEHOT) return fail(ctx, PG_ERR_UNSUPPORTED, "count export uses the histogram form");
-    int rc = run_prep(ctx, traj, bins);
+    int rc = run_prep(ctx, traj, bins, PG_FORM_HIST);
     if (rc) return rc;
     const SysGeom &g = ctx->geo;
     std::vector<PairTile> t((size_t)n_pairs);
@@ -1398,8 +1418,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         g.F = v.n_frames;
         g.ldb = bins_ld(g.F);
         for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
-        g.codes = 0;
-        g.codes = needs_row_codes(g) ? 1 : 0;
+        set_bin_layout(g, PG_FORM_HIST);
         L.prec = v.double_prec;
         L.own_cols = !v.on_device;
         L.ld = v.on_device ? v.ld : v.n_frames;
@@ -1530,6 +1549,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     key.push_back((int64_t)ctx->nfix_max);
     key.push_back(h32 ? (int64_t)(uintptr_t)ctx->scratch.p : -1);
     key.push_back(sys[0].g.codes);
+    key.push_back(sys[0].g.ilv);
     for (int k = 0; k < 6; k++) key.push_back(bins[k]);
     for (int s = 0; s < n_sys; s++) {
         const pg_bat_view &v = trajs[s];
@@ -1591,7 +1611,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
                                 st);
         }
         if (e == cudaSuccess)
-            e = h32 ? launch_pairs_hist32_batch(bmax, sys[0].g.codes != 0, (const SysDesc *)(meta + mo_sd),
+            e = h32 ? launch_pairs_hist32_batch(bmax, sys[0].g.codes != 0, sys[0].g.ilv != 0,
+                                                (const SysDesc *)(meta + mo_sd),
                                                 (const PairTile *)(meta + mo_t),
                                                 (const int *)(meta + mo_ts), (int64_t)tiles.size(),
                                                 (const unsigned long long *)ctx->nfix.p, ctx->nfix_scale,

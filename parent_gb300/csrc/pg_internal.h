@@ -28,12 +28,30 @@ struct SysGeom {
     int F;                     // frames
     int64_t ldb;               // bytes between DOF rows of the uint8 bin matrix (bins_ld(F))
     int bins[6];               // b1D a1D d1D b2D a2D d2D
-    int codes;                 // 1: a second D x ldb matrix follows the bin matrix, holding
+    int codes;                 // 1: a second matrix follows the bin matrix, holding
                                // each 2D bin b as the row code (b >> 1) | (b & 1) << 7
+    int ilv;                   // 1: both matrices are frame-group interleaved (ilv_index)
+                               // instead of DOF rows ldb bytes apart
 };
 
+// Frame-group interleaved bin layout (SysGeom::ilv), read by the streamed
+// 32-slot histogram kernel: frames in groups of 16, group k holds the 16
+// bytes of every DOF, DOF g at byte (k * ilv_dp(D) + g) * 16, so the bins
+// of consecutive DOFs for one group are contiguous (a tile's 4 row DOFs are
+// 64 bytes, its 8 column DOFs one 128-byte line). D is padded to a multiple
+// of 8 so that every group and every 8-DOF column block starts on a line.
+__host__ __device__ inline int64_t ilv_dp(int D) { return ((int64_t)D + 7) / 8 * 8; }
+__host__ __device__ inline int64_t ilv_groups(int F) { return ((int64_t)F + 15) / 16; }
+__host__ __device__ inline int64_t ilv_bytes(int D, int F) { return ilv_groups(F) * ilv_dp(D) * 16; }
+__host__ __device__ inline int64_t ilv_index(int64_t Dp, int g, int f) {
+    return ((int64_t)(f >> 4) * Dp + g) * 16 + (f & 15);
+}
+
 // Bytes of the bin matrix (and the row-code matrix after it, if any).
-inline size_t bins_bytes(const SysGeom &g) { return (size_t)g.D * (size_t)g.ldb * (g.codes ? 2 : 1); }
+inline size_t bins_bytes(const SysGeom &g) {
+    const size_t one = g.ilv ? (size_t)ilv_bytes(g.D, g.F) : (size_t)g.D * (size_t)g.ldb;
+    return one * (g.codes ? 2 : 1);
+}
 
 __host__ __device__ inline int dof_type(int g, int nb, int na) {
     return g < nb ? TB : (g < nb + na ? TA : TD);
@@ -155,7 +173,9 @@ cudaError_t launch_pairs_hist(const SysGeom &g, const uint8_t *bins, const DofAr
 int pairs_hist_config(int bmax, int *tile_dim, int *chunk_frames, int *stages);
 
 // 32-slot histogram pair kernel (2D bins <= 50): conflict-free counters over
-// 4 x 8-DOF tiles, persistent grid of pairs_hist32_grid(n) CTAs. Up to 35
+// 4 x 8-DOF tiles, persistent grid of pairs_hist32_grid(n) CTAs. Geometries
+// with the interleaved bin layout (SysGeom::ilv) run the streamed form (rows
+// loaded straight from global memory), the others the TMA-ring form. Up to 35
 // bins 32-bit counters; 36-50 bins 16-bit counters, which need the row-code
 // matrix (SysGeom::codes), and tiles that could overflow a 16-bit counter move
 // counts into a per-CTA overflow area in `scratch`
@@ -167,7 +187,7 @@ size_t pairs_hist32_scratch_bytes(int bmax, int grid);
 cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
                                 const unsigned long long *nfix, double fix, const PairTile *tiles, int64_t n_tiles,
                                 PairOut out, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
-cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, const PairTile *tiles,
+cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, bool ilv, const SysDesc *sys, const PairTile *tiles,
                                       const int *tile_sys, int64_t n_tiles, const unsigned long long *nfix,
                                       double fix, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st);
 

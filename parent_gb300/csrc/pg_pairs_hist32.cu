@@ -422,6 +422,257 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Streamed form of the same layouts. The TMA ring above makes every consumer
+// warp wait on, and release, every chunk of the tile: each warp only counts
+// fc/31 frames of a chunk, so the per-chunk synchronisation and the uneven
+// split of a chunk's 16-frame groups over 31 warps are paid for every few
+// hundred updates, and beside 160 KB of 16-bit counters only two 2,048-frame
+// stages fit. Here there is no ring: all 32 warps count, each streams its
+// own 16-frame groups (group k goes to warp k mod 32) straight from global
+// memory into registers, two groups ahead, from the frame-group interleaved
+// bin layout (ilv_index), in which one group of a tile's 4 row DOFs is 64
+// contiguous bytes and of its 8 column DOFs one 128-byte line, so a warp's
+// two 16-byte loads per group touch two lines. The warps meet only at the
+// end of a tile (and at the 16-bit folds). Counting, folds and the epilogue
+// are those of the ring kernel.
+constexpr int kFoldGroups = kFoldFrames / 16;
+
+// 16 bytes from global memory, not kept in L1 (each line is read once)
+__device__ __forceinline__ uint4 ldg_stream(const void *p) {
+    uint4 r;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(p));
+    return r;
+}
+
+// One lane's 16 updates of a whole group: row bins (W32) or row codes
+// (16-bit) in rv, column bins in cv; the same arithmetic as the ring kernel.
+template <bool W32>
+__device__ __forceinline__ void count_group(const uint4 rv, const uint4 cv, uint32_t Bc, uint32_t hbase,
+                                            uint32_t kw, uint32_t kneg) {
+    const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+    const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+    if (W32) {
+        uint32_t ad[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t sel = h ? 0x4342u : 0x4140u;
+                const uint32_t v = __byte_perm(rw[q], 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
+                const uint32_t hi = v >> 16;
+                ad[4 * q + 2 * h + 1] = hi * kw + hbase;
+                ad[4 * q + 2 * h] = v * kw + hbase + hi * kneg;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) red_add1_nc(ad[4 * q + k]);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t rs = rw[q] & 0x7f7f7f7fu;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const uint32_t sel = h ? 0x4342u : 0x4140u;
+                const uint32_t v = __byte_perm(rs, 0u, sel) * Bc + __byte_perm(cw[q], 0u, sel);
+                const uint32_t hi = v >> 16;
+                const uint32_t a_hi = hi * kw + hbase;
+                const uint32_t a_lo = v * kw + hbase + hi * kneg;
+                if (h == 0) {
+                    red_add_nc(a_lo, half_value<0>(rw[q]));
+                    red_add_nc(a_hi, half_value<1>(rw[q]));
+                } else {
+                    red_add_nc(a_lo, half_value<2>(rw[q]));
+                    red_add_nc(a_hi, half_value<3>(rw[q]));
+                }
+            }
+        }
+    }
+}
+
+template <bool W32>
+__global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid_constant__ Hist32Args a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int wpl = words_per_lane(a.bmax);
+    const int nwords = wpl * 32;
+    uint32_t *hist = (uint32_t *)smem;
+    __shared__ unsigned long long s_snl[32];
+    __shared__ unsigned int s_occ[32];
+    __shared__ int s_heavy[32];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid * 4; i < nwords; i += kThreads * 4) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < 32) {
+        s_snl[tid] = 0ull;
+        s_occ[tid] = 0u;
+        s_heavy[tid] = 0;
+    }
+    __syncthreads();
+
+    auto sys_of = [&](int64_t t) -> const SysDesc & { return a.tile_sys ? a.many[a.tile_sys[t]] : a.one; };
+    const int pr = lane / kCols, pc = lane % kCols;
+    const uint32_t hbase = smem_u32(hist) + lane * 4;
+    uint32_t *ovf = a.ovf_all + (size_t)blockIdx.x * 2 * nwords;  // [bin][lane]
+    for (int64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        const SysDesc &d = sys_of(t);
+        const PairTile tile = a.tiles[t];
+        const int F = d.geo.F, D = d.geo.D;
+        const int G = (F + 15) >> 4, Gfull = F >> 4;
+        const int64_t gstride = ilv_dp(D) * 16;
+        const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
+        const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
+        const bool valid = gr >= 0 && gc >= 0 && gr < gc;
+        const uint32_t Bc = valid ? (uint32_t)d.dof.b2[gc] : 0u;
+        // every warp holds all 32 slots, so this vote is the same in every
+        // warp (it decides who takes the fold barriers: all of them or none)
+        const bool risky = valid && (W32 ? false : d.dof.m2[gc] > 65535);
+        const bool folding = !W32 && __any_sync(0xffffffffu, risky) && G > kFoldGroups;
+        // rows: bins (32-bit counters) or row codes (16-bit), after the bins
+        const uint8_t *rp = (W32 ? d.bins : d.bins + ilv_bytes(D, F)) + (int64_t)(valid ? gr : 0) * 16;
+        const uint8_t *cp = d.bins + (int64_t)(valid ? gc : 0) * 16;
+        const int span = folding ? kFoldGroups : G;
+        for (int g0 = 0; g0 < G; g0 += span) {
+            const int gend = min(G, g0 + span);
+            const int fe = min(gend, Gfull);  // whole groups of this span end here
+            if (valid) {
+                int g = g0 + warp;
+                uint4 r0 = make_uint4(0u, 0u, 0u, 0u), c0 = r0, r1 = r0, c1 = r0;
+                if (g < fe) {
+                    r0 = ldg_stream(rp + (int64_t)g * gstride);
+                    c0 = ldg_stream(cp + (int64_t)g * gstride);
+                }
+                if (g + 32 < fe) {
+                    r1 = ldg_stream(rp + (int64_t)(g + 32) * gstride);
+                    c1 = ldg_stream(cp + (int64_t)(g + 32) * gstride);
+                }
+                for (; g < fe; g += 32) {
+                    const uint4 r = r0, c = c0;
+                    r0 = r1;
+                    c0 = c1;
+                    if (g + 64 < fe) {
+                        r1 = ldg_stream(rp + (int64_t)(g + 64) * gstride);
+                        c1 = ldg_stream(cp + (int64_t)(g + 64) * gstride);
+                    }
+                    count_group<W32>(r, c, Bc, hbase, a.kw, a.kneg);
+                }
+                // the ragged last group of the trajectory, on the warp whose
+                // turn it is
+                if (Gfull < gend && Gfull >= g0 && ((Gfull - g0) & 31) == warp) {
+                    const uint4 rv = ldg_stream(rp + (int64_t)Gfull * gstride);
+                    const uint4 cv = ldg_stream(cp + (int64_t)Gfull * gstride);
+                    const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+                    const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                    const int n = F - Gfull * 16;
+#pragma unroll
+                    for (int k = 0; k < 16; k++) {
+                        if (k < n) {
+                            const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                            const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
+                            if (W32) red_add1_nc(hbase + ((br * Bc + bc) << 7));
+                            else red_add_nc(hbase + (((br & 0x7fu) * Bc + bc) << 7), (br & 0x80u) ? 0xFFFF0001u : 1u);
+                        }
+                    }
+                }
+            }
+            if (folding && gend < G) {
+                // every warp's reductions so far are done; move both counts of
+                // every word whose low half reached 32,768 out (w & 31 == lane)
+                __syncthreads();
+                for (int w = tid; w < nwords; w += kThreads) {
+                    const uint32_t v = hist[w];
+                    if (v & 0x8000u) {
+                        const uint32_t n_odd = (0u - (v >> 16)) & 0xffffu, n_even = (v & 0xffffu) - n_odd;
+                        hist[w] = 0u;
+                        const int b = (w >> 5) * 2;
+                        ovf[b * 32 + lane] += n_even;
+                        ovf[(b + 1) * 32 + lane] += n_odd;
+                        s_heavy[lane] = 1;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+
+        // ---- epilogue: this thread reads words j = warp, warp + 32, ... of
+        // slot `lane`, zeroing them
+        unsigned long long snl = 0ull;
+        int occ = 0;
+        if (valid && W32) {
+            const int nbin = d.dof.b2[gr] * d.dof.b2[gc];
+            int64_t *dump = d.out.counts ? d.out.counts + (t * 32 + lane) * d.out.counts_bmax * d.out.counts_bmax
+                                         : nullptr;
+            for (int j = warp; j < nbin; j += kWarps) {
+                const int w = j * 32 + lane;
+                const uint32_t n = hist[w];
+                hist[w] = 0u;
+                snl += __ldg(a.nfix + n);
+                occ += n != 0u;
+                if (dump) dump[j] = n;
+            }
+            atomicAdd(&s_snl[lane], snl);
+            atomicAdd(&s_occ[lane], (unsigned int)occ);
+        } else if (valid) {
+            // word j = h * Bc + c holds bins (2h, c) and (2h + 1, c)
+            const int Br = d.dof.b2[gr], Bcc = d.dof.b2[gc];
+            const int nw = (Br + 1) / 2 * Bcc;
+            const bool heavy = s_heavy[lane] != 0;
+            int64_t *dump = d.out.counts ? d.out.counts + (t * 32 + lane) * d.out.counts_bmax * d.out.counts_bmax
+                                         : nullptr;
+            for (int j = warp; j < nw; j += kWarps) {
+                const int w = j * 32 + lane;
+                const uint32_t v = hist[w];
+                hist[w] = 0u;
+                uint32_t n1 = (0u - (v >> 16)) & 0xffffu;  // odd row bin
+                uint32_t n0 = (v & 0xffffu) - n1;           // even row bin
+                if (heavy) {
+                    uint32_t *o = ovf + (size_t)(2 * j) * 32 + lane;
+                    const uint32_t o0 = o[0], o1 = o[32];
+                    if (o0 | o1) {
+                        n0 += o0;
+                        n1 += o1;
+                        o[0] = 0u;
+                        o[32] = 0u;
+                    }
+                }
+                snl += __ldg(a.nfix + n0) + __ldg(a.nfix + n1);
+                occ += (n0 != 0u) + (n1 != 0u);
+                if (dump) {
+                    const int h = j / Bcc, c = j - h * Bcc;
+                    dump[2 * h * Bcc + c] = n0;
+                    if (2 * h + 1 < Br) dump[(2 * h + 1) * Bcc + c] = n1;
+                }
+            }
+            atomicAdd(&s_snl[lane], snl);
+            atomicAdd(&s_occ[lane], (unsigned int)occ);
+        }
+        __syncthreads();
+        if (tid < 32) {
+            if (valid) {
+                const double N = (double)F;
+                const double sn = (double)s_snl[tid] / a.fix;
+                const int o = (int)s_occ[tid];
+                const double S2 = d.lnN + d.dof.acon[gr] + d.dof.acon[gc] - sn / N + (o - 1.0) / (2.0 * N);
+                if (d.out.par) d.out.par[par_pair_index(d.out.L, d.geo.nb, d.geo.na, d.geo.nd, gr, gc)] = S2;
+                if (d.out.mi) {
+                    const double mi = d.dof.s1[gr] + d.dof.s1[gc] - S2;
+                    d.out.mi[(int64_t)gr * d.geo.D + gc] = mi;
+                    d.out.mi[(int64_t)gc * d.geo.D + gr] = mi;
+                }
+            }
+            // the next tile's epilogue atomics come after its first barrier
+            s_snl[tid] = 0ull;
+            s_occ[tid] = 0u;
+            s_heavy[tid] = 0;
+        }
+    }
+}
+
 int sm_count() {
     static int n = 0;
     if (n == 0) {
@@ -459,7 +710,7 @@ bool config(int bmax, int *fc, int *nst) {
 
 // codes: the row-code matrix follows every system's bin matrix (required by
 // the 16-bit layout)
-cudaError_t launch(Hist32Args &a, bool codes, void *scratch, size_t scratch_bytes, cudaStream_t st) {
+cudaError_t launch(Hist32Args &a, bool codes, bool streamed, void *scratch, size_t scratch_bytes, cudaStream_t st) {
     if (!config(a.bmax, &a.fc, &a.nst)) return cudaErrorInvalidValue;
     if (!wide_counters(a.bmax) && !codes) return cudaErrorInvalidValue;
     if (a.n_tiles <= 0) return cudaSuccess;
@@ -471,13 +722,14 @@ cudaError_t launch(Hist32Args &a, bool codes, void *scratch, size_t scratch_byte
     a.ovf_all = (uint32_t *)scratch;
     a.kw = 128u;
     a.kneg = 0u - (128u << 16);
-    const size_t smem = smem_bytes(a.bmax, a.fc, a.nst);
+    const size_t smem = streamed ? hist32_bytes(a.bmax) : smem_bytes(a.bmax, a.fc, a.nst);
     auto go = [&](auto kern) -> cudaError_t {
         cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e2 != cudaSuccess) return e2;
         kern<<<grid, kThreads, smem, st>>>(a);
         return cudaGetLastError();
     };
+    if (streamed) return wide_counters(a.bmax) ? go(pairs_hist32s_kernel<true>) : go(pairs_hist32s_kernel<false>);
     return wide_counters(a.bmax) ? go(pairs_hist32_kernel<true>) : go(pairs_hist32_kernel<false>);
 }
 
@@ -521,7 +773,7 @@ cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const Dof
     int bmax = 1;
     for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
     if (!pairs_hist32_supported(bmax)) return cudaErrorInvalidValue;
-    if (g.ldb < bins_ld(g.F)) return cudaErrorInvalidValue;
+    if (!g.ilv && g.ldb < bins_ld(g.F)) return cudaErrorInvalidValue;
     Hist32Args a{};
     a.one.geo = g;
     a.one.bins = bins;
@@ -534,10 +786,10 @@ cudaError_t launch_pairs_hist32(const SysGeom &g, const uint8_t *bins, const Dof
     a.fix = fix;
     a.err = err;
     a.bmax = bmax;
-    return launch(a, g.codes != 0, scratch, scratch_bytes, st);
+    return launch(a, g.codes != 0, g.ilv != 0, scratch, scratch_bytes, st);
 }
 
-cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, const PairTile *tiles,
+cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, bool ilv, const SysDesc *sys, const PairTile *tiles,
                                       const int *tile_sys, int64_t n_tiles, const unsigned long long *nfix,
                                       double fix, int *err, void *scratch, size_t scratch_bytes, cudaStream_t st) {
     if (!pairs_hist32_supported(bmax)) return cudaErrorInvalidValue;
@@ -550,7 +802,7 @@ cudaError_t launch_pairs_hist32_batch(int bmax, bool codes, const SysDesc *sys, 
     a.fix = fix;
     a.err = err;
     a.bmax = bmax;
-    return launch(a, codes, scratch, scratch_bytes, st);
+    return launch(a, codes, ilv, scratch, scratch_bytes, st);
 }
 
 }  // namespace pg

@@ -275,9 +275,14 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const double mn = s_mn, mx = s_mx;
     const double bs1 = __ddiv_rn(__dsub_rn(mx, mn), (double)B1);
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
-    uint8_t *brow = bins + (int64_t)g * geo.ldb;
-    // row codes for the 16-bit 32-slot histogram layout: (b >> 1) | (b & 1) << 7
-    uint8_t *crow = geo.codes ? bins + ((int64_t)geo.D + g) * geo.ldb : nullptr;
+    // DOF rows ldb bytes apart, or the frame-group interleaved layout
+    // (ilv_index) of the streamed 32-slot histogram kernel
+    const int64_t Dp = ilv_dp(geo.D);
+    uint8_t *brow = geo.ilv ? bins + (int64_t)g * 16 : bins + (int64_t)g * geo.ldb;
+    // row codes for the 16-bit 32-slot histogram layouts: (b >> 1) | (b & 1) << 7
+    uint8_t *crow = !geo.codes ? nullptr
+                    : (geo.ilv ? bins + ilv_bytes(geo.D, F) + (int64_t)g * 16
+                               : bins + ((int64_t)geo.D + g) * geo.ldb);
     int bad = 0;
     {
         // d = fl64(x' - mn) (x' the shifted value for dihedrals) is formed in
@@ -319,8 +324,9 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
             atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
-            brow[f] = (uint8_t)i2;
-            if (crow) crow[f] = (uint8_t)((i2 >> 1) | ((i2 & 1) << 7));
+            const int64_t at = geo.ilv ? ((int64_t)(f >> 4) * Dp) * 16 + (f & 15) : (int64_t)f;
+            brow[at] = (uint8_t)i2;
+            if (crow) crow[at] = (uint8_t)((i2 >> 1) | ((i2 & 1) << 7));
         }
     }
     if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);

@@ -53,11 +53,15 @@ def test_batch_matches_oracle(eng, bins):
     _check_against_oracle(trajs, bodies, trees, bins)
 
 
-@pytest.mark.parametrize("slots", ["16", "32"])
+@pytest.mark.parametrize("slots", ["16", "32", "stream"])
 def test_batch_both_histogram_layouts_at_50_bins(eng, monkeypatch, slots):
     """At 50 bins the batch runs the 16-slot layout or, forced, the 32-slot
-    layout with 16-bit counters (row codes written per system)."""
-    monkeypatch.setenv("PG_HIST_SLOTS", slots)
+    layout with 16-bit counters (row codes written per system), ring-fed or
+    streamed from each system's interleaved bin matrices."""
+    if slots == "stream":
+        monkeypatch.setenv("PG_HIST_STREAM", "1")
+    else:
+        monkeypatch.setenv("PG_HIST_SLOTS", slots)
     bins = (50, 50, 50, 50, 47, 39)
     # not the one-frame system: its MI values are rounding noise around 0,
     # so its tree order is not defined by the data

@@ -20,7 +20,10 @@ from oracle import check
 pytestmark = pytest.mark.gpu
 
 
-def _run(n_atoms, frames, bins, form="auto", seed=20261, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05):
+def _run(n_atoms, frames, bins, form="auto", seed=20261, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05,
+         monkeypatch=None, stream=False):
+    if stream:
+        monkeypatch.setenv("PG_HIST_STREAM", "1")
     t = pg.synth_host(n_atoms, frames, double_prec=0, seed=seed, frac_bimodal_dih=frac_bimodal_dih,
                       frac_bimodal_bond=frac_bimodal_bond)
     with pg.Engine(0) as eng:
@@ -42,16 +45,18 @@ def _assert_ok(res):
     assert res["mist_max_abs_dMI_nats"] <= 1e-9, res
 
 
-def test_precision_path_system_matches_oracle_at_50_bins():
-    res, used = _run(1000, 100_000, (50,) * 6)
+@pytest.mark.parametrize("stream", [False, True])
+def test_precision_path_system_matches_oracle_at_50_bins(monkeypatch, stream):
+    res, used = _run(1000, 100_000, (50,) * 6, monkeypatch=monkeypatch, stream=stream)
     assert used == "hist"
     assert res["pairs_total"] == 2994 * 2993 // 2 and res["mist_edges"] == 2993
     _assert_ok(res)
 
 
-def test_precision_path_system_matches_oracle_at_30_bins():
-    # the 32-slot layout with 32-bit counters
-    res, used = _run(1000, 100_000, (30,) * 6, seed=777)
+@pytest.mark.parametrize("stream", [False, True])
+def test_precision_path_system_matches_oracle_at_30_bins(monkeypatch, stream):
+    # the 32-slot layout with 32-bit counters, ring-fed or streamed
+    res, used = _run(1000, 100_000, (30,) * 6, seed=777, monkeypatch=monkeypatch, stream=stream)
     assert used == "hist"
     _assert_ok(res)
 

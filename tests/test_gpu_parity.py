@@ -268,14 +268,17 @@ def test_mist_over_a_cluster_matches_oracle(eng, monkeypatch, cluster):
     compare_mist(e, tot, re, rt)
 
 
-@pytest.mark.parametrize("groups", ["4", "16"])
+@pytest.mark.parametrize("groups", ["4", "16", "4-stream"])
 def test_grouped_upload_schedule_matches(eng, monkeypatch, groups):
     """PG_STREAM_GROUPS > 1 (uploads in DOF groups on the copy stream, pair
     launches alternating between two streams) gives the same body, bit for
-    bit, as the default one-group upload."""
+    bit, as the default one-group upload; also with the streamed 32-slot
+    layout (its integer n ln n sums equal the other layouts' bit for bit)."""
     t = _synth_case(150, 6000, 0, seed=23, frac_bimodal_dih=0.2)
     base = eng.entropy(t, (50,) * 6, "hist").flat()
-    monkeypatch.setenv("PG_STREAM_GROUPS", groups)
+    monkeypatch.setenv("PG_STREAM_GROUPS", groups.split("-")[0])
+    if groups.endswith("stream"):
+        monkeypatch.setenv("PG_HIST_STREAM", "1")
     assert np.array_equal(eng.entropy(t, (50,) * 6, "hist").flat(), base)
 
 
@@ -384,11 +387,15 @@ def test_large_properties(eng):
 @pytest.mark.parametrize("n_atoms,F,bins", [(40, 70000, (50,) * 6), (20, 3000, (10, 20, 30, 50, 20, 8)),
                                             (30, 20000, (30,) * 6), (25, 5000, (20, 30, 35, 35, 20, 8)),
                                             (22, 4001, (50, 50, 50, 37, 49, 41)), (14, 999, (5, 5, 5, 36, 1, 3))])
-def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins):
+@pytest.mark.parametrize("feed", ["ring", "stream"])
+def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins, feed):
     """The 32-slot histogram layout (32-bit counters up to 35 bins, 16-bit
     counters for row-bin pairs above, odd row-bin counts included) gives the
-    same counts and values."""
+    same counts and values, fed by the TMA ring or streamed from the
+    frame-group interleaved bin matrix (ragged last groups included)."""
     monkeypatch.setenv("PG_HIST_SLOTS", "32")
+    if feed == "stream":
+        monkeypatch.setenv("PG_HIST_STREAM", "1")
     t = _synth_case(n_atoms, F, 0, seed=n_atoms + F, frac_bimodal_dih=0.2)
     body = eng.entropy(t, bins, "hist")
     ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
@@ -567,12 +574,16 @@ def test_hist16_layout_matches_oracle(eng, monkeypatch):
         assert np.array_equal(x, y), p
 
 
-@pytest.mark.parametrize("slots", ["32", "16"])
+@pytest.mark.parametrize("slots", ["32", "16", "stream"])
 def test_peaked_counts_above_16_bits(eng, monkeypatch, slots):
     """Pairs of DOFs that sit on one value in the same 70% of 150,000 frames:
     one 2D bin holds 105,000 counts, above a 16-bit counter, so the 32-slot
-    layout has to move counts out during the run. Counts stay bit-exact."""
-    monkeypatch.setenv("PG_HIST_SLOTS", slots)
+    layouts (ring-fed and streamed) have to move counts out during the run.
+    Counts stay bit-exact."""
+    if slots == "stream":
+        monkeypatch.setenv("PG_HIST_STREAM", "1")
+    else:
+        monkeypatch.setenv("PG_HIST_SLOTS", slots)
     rng = np.random.default_rng(5)
     n_dih, F = 5, 150000
     t = pg.synth_host(n_dih + 3, F, double_prec=0, seed=77)
