@@ -114,6 +114,9 @@ def parse():
                     help="pairs of the timed system checked against the FP64 oracle after the timed region "
                          "(plus bit-exact counts on 100 of them and the oracle's MIST on the GPU's body)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-size parity leg")
+    ap.add_argument("--compare-forms", choices=["auto", "on", "off"], default="auto",
+                    help="time one step of each form (tensor-core one-hot, shared-memory histogram) at 50 and "
+                         "10 bins after the timed region (auto: on for the protein-dimer workload)")
     ap.add_argument("--batconv", action="store_true",
                     help="instead of the step: time the Cartesian -> BAT conversion of a synthetic chain "
                          "with the workload's atoms and frames (host coordinates in, device columns out)")
@@ -553,6 +556,12 @@ def run_gb300(args):
                "breakdown": parts[-1]}
         pg._check(pg.lib().pg_host_free_pinned(hout))
 
+    # ---- the metric's own comparison: each form at 50 and 10 bins (after the timed region)
+    forms_cmp = None
+    want_cmp = args.compare_forms == "on" or (args.compare_forms == "auto" and args.workload == DEFAULT)
+    if want_cmp and rank == 0:
+        forms_cmp = compare_forms(eng, view, n_dih, units, stream)
+
     # ---- full-size parity of the timed system itself (outside every timed region)
     parity_full = None
     if want_parity:
@@ -609,6 +618,7 @@ def run_gb300(args):
             "kernel_ms": {"prep": statistics.mean(prep_ms), "pairs": statistics.mean(pair_ms),
                           "mist": statistics.mean(mist_ms)},
             "roofline": roofline, "roofline_prep": roofline_prep,
+            "onehot_vs_hist": forms_cmp,
             "cpu_baseline": cpu, "parity": parity_full, "parity_cpu_sample": parity, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk,
         }
@@ -618,6 +628,47 @@ def run_gb300(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def compare_forms(eng, view, n_dih: int, units: int, stream):
+    """One step (pg_entropy + pg_mist, device-resident columns) of each form at
+    50 and 10 bins, timed with CUDA events on the library's stream: the
+    comparison the metric names (tensor-core one-hot against shared-memory
+    histogram). The one-hot form's roofline is 2*B^2 FLOPs per update against
+    the dense FP8 rate, taken as 2x the measured sustained cuBLAS bf16 rate
+    (these are seconds-long kernels)."""
+    import torch
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    fp8 = 2.0 * float(peaks.get("bf16_tflops_sustained", 1700.0))
+    out = {"peak_fp8_tflops": fp8, "peak_note": "2x measured sustained cuBLAS bf16 (MEASURED_PEAKS.json)"}
+    for b in (50, 10):
+        row = {}
+        for form in ("hist", "onehot"):
+            eng.entropy(view, (b,) * 6, form, keep_result=False)  # first call of this geometry: buffers
+            eng.mist(n_dih)
+            eng.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            eng.entropy(view, (b,) * 6, form, keep_result=False)
+            pair_ms = float(eng.timings()[1])
+            eng.mist(n_dih)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            r = {"ms_per_step": ms, "pairs_ms": pair_ms, "value": units / (ms / 1e3), "form": eng.last_form()}
+            if form == "onehot":
+                tf = 2.0 * b * b * units / (pair_ms / 1e3) / 1e12
+                r["roofline"] = {"bound": "tensor", "achieved": tf, "peak": fp8, "unit": "TFLOP/s", "frac": tf / fp8}
+            row[form] = r
+        row["hist_over_onehot_time"] = row["hist"]["ms_per_step"] / row["onehot"]["ms_per_step"]
+        out[str(b)] = row
+    out["target"] = "one-hot >= 3x less wall time than the histogram form at 50 bins"
+    out["target_met"] = bool(out["50"]["hist_over_onehot_time"] >= 3.0)
+    return out
 
 
 def full_parity(args, eng, view, host_ptr: int, n_dih: int, F: int, prec: int, bins):

@@ -44,7 +44,7 @@ CU_SOURCES = {
     "pg_batconv.cu": ["--fmad=false"],
     "pg_mie.cu": [],
 }
-CPP_SOURCES = ["pg_io.cpp"]
+CPP_SOURCES = ["pg_io.cpp", "pg_io_compat.cpp"]
 CLIS = ["PARENT_gb300", "get_PAR_MIST_gb300", "get_PAR_MIE_gb300", "get_PAR_info_gb300"]
 
 
@@ -79,7 +79,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     BINDIR.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.h")) + [INCLUDE / "parent_gb300.h"]
+    headers = sorted(CSRC.glob("*.h")) + [INCLUDE / "parent_gb300.h", INCLUDE / "parent_gb300_io.h"]
     steps = []
     objs = []
     for src, extra in CU_SOURCES.items():

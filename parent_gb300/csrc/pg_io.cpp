@@ -54,6 +54,50 @@ int ioerr(int code, const char *fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+namespace pg {
+
+// The header field checks of read_BAT_header (io_binary.cpp:127-145) and
+// read_PAR_header (io_binary.cpp:477-519, :554-591), with the reference's
+// messages on stderr. They return PG_OK or PG_ERR_FORMAT.
+int check_bat_fields(int version, int prec, int n_dih, int n_frames) {
+    if (version < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", version);
+    if (prec != 0 && prec != 1)
+        return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!", prec);
+    if (n_dih > 19997)
+        fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n",
+                n_dih + 3);
+    if (n_dih < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", n_dih);
+    if (n_frames < 1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", n_frames);
+    return PG_OK;
+}
+
+// bins in file order: b1D a1D d1D b2D a2D d2D
+int check_par_fields(int version, int prec, int n_dih, int n_frames, const int bins[6]) {
+    const int rc = check_bat_fields(version, prec, n_dih, n_frames);
+    if (rc) return rc;
+    static const char *nm[6] = {"BONDS IN 1D", "ANGLES IN 1D", "DIHEDRALS IN 1D", "BONDS IN 2D", "ANGLES IN 2D",
+                                "DIHEDRALS IN 2D"};
+    for (int k = 0; k < 6; k++)
+        if (bins[k] < 1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER BINS FOR %s (%d) < 1!", nm[k], bins[k]);
+    return PG_OK;
+}
+
+// one dihedral entry of a .par header (atoms, type, parent)
+int check_par_dihedral(const int d[6]) {
+    for (int k = 0; k < 4; k++)
+        if (d[k] < 1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL ID < 1 !");
+    if (!(d[4] == 1 || d[4] == 0 || d[4] == -1))
+        return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL TYPE NEITHER 0, 1 NOR -1 !");
+    if (d[5] < -1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL IS PHASEANGLE OF A DIHEDRAL WITH NEGATIVE ID !");
+    return PG_OK;
+}
+
+}  // namespace pg
+
+namespace {
+
 struct Header {
     int version = 3, double_prec = 1, n_dih = 0, n_frames = 0;
     std::vector<std::string> residues, atoms, molecules;
@@ -159,16 +203,8 @@ extern "C" {
 static int read_bat_header(FILE *f, Header &h, const char *path) {
     if (!rd(f, &h.version, 4) || !rd(f, &h.double_prec, 4) || !rd(f, &h.n_dih, 4) || !rd(f, &h.n_frames, 4))
         return ioerr(PG_ERR_IO, "ERROR: could not read the header of %s", path);
-    // the checks of read_BAT_header, io_binary.cpp:127-145
-    if (h.version < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version);
-    if (h.double_prec != 0 && h.double_prec != 1)
-        return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!",
-                     h.double_prec);
-    if (h.n_dih > 19997)
-        fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n",
-                h.n_dih + 3);
-    if (h.n_dih < 0) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih);
-    if (h.n_frames < 1) return ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames);
+    const int rc = pg::check_bat_fields(h.version, h.double_prec, h.n_dih, h.n_frames);
+    if (rc) return rc;
     if (h.version >= 3) {
         if (!read_atoms(f, h)) return ioerr(PG_ERR_IO, "ERROR: truncated atom block in %s", path);
     } else {
@@ -516,15 +552,7 @@ PG_API int pg_par_read(const char *path, pg_par **out) {
         int hv[4];
         if (!rd(f, hv, 16) || !rd(f, p->bins, 24)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
         h.version = hv[0]; h.double_prec = hv[1]; h.n_dih = hv[2]; h.n_frames = hv[3];
-        // the checks of read_PAR_header, io_binary.cpp:477-519
-        if (h.version < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. VERSION NUMBER (%d) < 0!", h.version); break; }
-        if (h.double_prec != 0 && h.double_prec != 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DOUBLE PRECISION VALUE (%d) NEITHER 0 NOR 1!", h.double_prec); break; }
-        if (h.n_dih > 19997) fprintf(stderr, "WARNING: %d ATOMS DECLARED IN THE FILE HEADER (CORRUPTED?). THIS WILL LEAD TO LARGE OUTPUT.\n", h.n_dih + 3);
-        if (h.n_dih < 0) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF DIHEDRALS (%d) < 0!", h.n_dih); break; }
-        if (h.n_frames < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER OF FRAMES (%d) < 1!", h.n_frames); break; }
-        static const char *nm[6] = {"BONDS IN 1D", "ANGLES IN 1D", "DIHEDRALS IN 1D", "BONDS IN 2D", "ANGLES IN 2D", "DIHEDRALS IN 2D"};
-        for (int k = 0; k < 6 && rc == PG_OK; k++)
-            if (p->bins[k] < 1) rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. NUMBER BINS FOR %s (%d) < 1!", nm[k], p->bins[k]);
+        rc = pg::check_par_fields(h.version, h.double_prec, h.n_dih, h.n_frames, p->bins);
         if (rc) break;
         if (h.version >= 3) {
             if (!read_atoms(f, h)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
@@ -534,12 +562,8 @@ PG_API int pg_par_read(const char *path, pg_par **out) {
         h.dih.resize((size_t)6 * h.n_dih);
         for (int i = 0; i < h.n_dih && rc == PG_OK; i++) {  // io_binary.cpp:554-596
             if (!rd(f, &h.dih[6 * i], 24)) { rc = ioerr(PG_ERR_IO, "ERROR READING HEADER OF FILE %s !", path); break; }
-            for (int k = 0; k < 4; k++)
-                if (h.dih[6 * i + k] < 1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL ID < 1 !"); break; }
+            rc = pg::check_par_dihedral(&h.dih[6 * i]);
             if (rc) break;
-            const int ty = h.dih[6 * i + 4];
-            if (!(ty == 1 || ty == 0 || ty == -1)) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL TYPE NEITHER 0, 1 NOR -1 !"); break; }
-            if (h.dih[6 * i + 5] < -1) { rc = ioerr(PG_ERR_FORMAT, "ERROR: FILE HEADER CORRUPTED. DIHEDRAL IS PHASEANGLE OF A DIHEDRAL WITH NEGATIVE ID !"); break; }
             if (h.version == 1 && h.dih[6 * i + 5] != -1) h.dih[6 * i + 5]++;
         }
         if (rc) break;
