@@ -175,10 +175,11 @@ PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_sh
  * list, the trees in one launch (one CTA per system), and the whole device
  * sequence is captured once into a CUDA graph that later calls with the same
  * geometry replay. outs (n_sys bodies), edges (n_sys arrays of D_s-1) and
- * totals (10 per system) may each be NULL. Histogram form; with
- * PG_FORM_AUTO and bin counts where the autotuner picks the one-hot form for
- * every system (up to 15 bins), the systems run one after another through
- * the one-hot form instead (same outputs). */
+ * totals (10 per system) may each be NULL. One form for the whole batch:
+ * PG_FORM_HIST, PG_FORM_ONEHOT (every system's tensor-core tiles in one
+ * launch, tiles naming their system; PG_ERR_UNSUPPORTED if a system's bins
+ * or frames are outside the one-hot form's range), or PG_FORM_AUTO (the
+ * one-hot form where the autotuner picks it for every system). */
 PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, const int bins[6], int form,
                             pg_par_body *outs, pg_mist_edge *const *edges, double *totals);
 
@@ -187,6 +188,16 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
  * ms[0] = preprocessing (extrema, modfit, binning, 1D), ms[1] = pair kernel,
  * ms[2] = MIST kernel, ms[3] = host<->device copies, ms[4] = whole call. */
 PG_API int pg_last_timings(const pg_ctx *ctx, double ms[5]);
+/* The autotuner's prediction (no reference counterpart) of the pair-kernel
+ * milliseconds of a system of n_dihedrals / n_frames at these bins in a form
+ * (PG_FORM_HIST with the histogram layout the library picks, PG_FORM_ONEHOT,
+ * or PG_FORM_AUTO: the form the autotuner picks). The model is ceil(tiles /
+ * concurrent tiles) x (t0 + t1 F) plus the form's per-call set-up, with t0,
+ * t1 and the set-up measured on this GPU by short probe launches the first
+ * time a kernel variant is needed (random bins, one full wave, F = 4,096 and
+ * 32,768). PG_ERR_UNSUPPORTED if the form cannot run the geometry. */
+PG_API int pg_predict_pair_ms(pg_ctx *ctx, int n_dihedrals, int n_frames, const int bins[6], int form,
+                              double *ms);
 /* Kernel launches issued by this context since creation. */
 PG_API int64_t pg_launch_count(const pg_ctx *ctx);
 /* Form used by the last pg_entropy (PG_FORM_HIST or PG_FORM_ONEHOT). */

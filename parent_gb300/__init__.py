@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
         "pg_launch_count": (i64, [vp]),
         "pg_last_form": (i, [vp]),
         "pg_stream": (vp, [vp]),
+        "pg_predict_pair_ms": (i, [vp, i, i, C.POINTER(C.c_int), i, dp]),
         "pg_pair_counts": (i, [vp, C.POINTER(BatView), C.POINTER(C.c_int), i, i, C.POINTER(C.c_int),
                                C.POINTER(C.c_int), C.POINTER(C.c_int64), i64]),
         "pg_dof_stats": (i, [vp, dp, dp, dp]),
@@ -370,6 +371,13 @@ class Engine:
             B1, B2 = bins[3 + tb(a)], bins[3 + tb(c)]
             res.append(out[k, :B1 * B2].reshape(B1, B2).copy())
         return res
+
+    def predict_pair_ms(self, n_dih: int, n_frames: int, bins, form: str = "auto") -> float:
+        """The autotuner's predicted pair-kernel milliseconds for a geometry."""
+        ms = C.c_double()
+        _check(lib().pg_predict_pair_ms(self._ctx, n_dih, n_frames, (C.c_int * 6)(*bins), FORMS[form],
+                                        C.byref(ms)), self._ctx)
+        return ms.value
 
     def dof_stats(self, D: int):
         mn, mx, sh = (np.zeros(D) for _ in range(3))

@@ -43,6 +43,7 @@ CU_SOURCES = {
     "pg_ingest.cu": [],
     "pg_batconv.cu": ["--fmad=false"],
     "pg_mie.cu": [],
+    "pg_autotune.cu": [],
 }
 CPP_SOURCES = ["pg_io.cpp", "pg_io_compat.cpp"]
 CLIS = ["PARENT_gb300", "get_PAR_MIST_gb300", "get_PAR_MIE_gb300", "get_PAR_info_gb300"]

@@ -25,7 +25,6 @@ size_t synth_scratch_bytes(const pg_synth_spec *sp, size_t *lat_bytes, size_t *s
                            std::vector<float> &lat, std::vector<int> &sw, std::vector<int> &sw_off);
 cudaError_t launch_synth_dev(const pg_synth_spec *sp, void *b, void *a, void *d, int64_t ld,
                              const float *lat, const int *sw, const int *sw_off, cudaStream_t st);
-int autotune_form(const SysGeom &g);
 void set_global_error(const char *msg);
 double probe_smem_red_rate(int n_sm, cudaStream_t st, int *launches);
 
@@ -115,7 +114,7 @@ struct pg_ctx {
     SysGeom geo{};
     // batched runs: one arena for every system's device data, descriptors,
     // and the CUDA graph of the last batch geometry
-    DevBuf batch, batchmeta;
+    DevBuf batch, batchmeta, ohbatch;
     cudaGraphExec_t graph = nullptr;
     std::vector<int64_t> graph_key;
     // host trajectories: uploads run on their own stream, one event per DOF group
@@ -325,25 +324,6 @@ static int ensure_fix_table(pg_ctx *ctx, int F) {
     return PG_OK;
 }
 
-// Histogram layouts: the 16-slot kernel (two lanes per pair), the 32-slot
-// kernel fed by a TMA ring, and the streamed 32-slot kernel (rows loaded
-// straight from the frame-group interleaved bin matrix).
-enum { HIST16 = 0, HIST32_RING = 1, HIST32_STREAM = 2 };
-
-// From measured inner-loop rates: the 32-slot ring kernel with 32-bit
-// counters (one wavefront per warp-wide reduction) for 2D bin counts up to
-// 35; the 16-slot kernel above that, where the 32-slot kernels need 16-bit
-// counters. PG_HIST_SLOTS=16 or 32 forces the 16-slot or the 32-slot ring
-// layout (32 slots up to 50 bins); PG_HIST_STREAM=1 the streamed one.
-static int hist_layout(const SysGeom &g) {
-    const int bm = bmax_of(g);
-    const char *e = getenv("PG_HIST_SLOTS");
-    const char *st = getenv("PG_HIST_STREAM");
-    if (e && atoi(e) == 16) return HIST16;
-    if (st && atoi(st) == 1 && pairs_hist32_supported(bm)) return HIST32_STREAM;
-    if (e && atoi(e) == 32) return pairs_hist32_supported(bm) ? HIST32_RING : HIST16;
-    return pairs_hist32_wide(bm) ? HIST32_RING : HIST16;
-}
 static bool use_hist32(const SysGeom &g) { return hist_layout(g) != HIST16; }
 
 // The bin matrices the preprocessing writes for a form: the 16-bit 32-slot
@@ -1252,6 +1232,31 @@ PG_API int pg_synth_device(pg_ctx *ctx, const pg_synth_spec *spec, void *bonds, 
     return PG_OK;
 }
 
+PG_API int pg_predict_pair_ms(pg_ctx *ctx, int n_dihedrals, int n_frames, const int bins[6], int form,
+                              double *ms) {
+    if (!ctx || !bins || !ms || n_dihedrals < 0 || n_frames < 1) return fail(ctx, PG_ERR_ARG, "bad arguments");
+    if (form != PG_FORM_HIST && form != PG_FORM_ONEHOT && form != PG_FORM_AUTO)
+        return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    CK(cudaSetDevice(ctx->device));
+    SysGeom g{};
+    g.n_dih = n_dihedrals;
+    g.nb = g.n_dih + 2;
+    g.na = g.n_dih + 1;
+    g.nd = g.n_dih;
+    g.D = g.nb + g.na + g.nd;
+    g.F = n_frames;
+    g.ldb = bins_ld(g.F);
+    for (int k = 0; k < 6; k++) {
+        if (bins[k] < 1 || (k >= 3 && bins[k] > PG_MAX_BINS_2D)) return fail(ctx, PG_ERR_ARG, "bad bin count");
+        g.bins[k] = bins[k];
+    }
+    const int f = form == PG_FORM_AUTO ? autotune_form(g) : form;
+    const double s = predict_pair_seconds(g, f);
+    if (s < 0.0) return fail(ctx, PG_ERR_UNSUPPORTED, "no prediction for this form and geometry");
+    *ms = s * 1e3;
+    return PG_OK;
+}
+
 PG_API int pg_probe_smem_red_rate(pg_ctx *ctx, double *reductions_per_s) {
     if (!ctx || !reductions_per_s) return fail(ctx, PG_ERR_ARG, "null argument");
     CK(cudaSetDevice(ctx->device));
@@ -1347,9 +1352,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     ctx->err.clear();
     cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
     if (n_sys < 1 || !trajs || !bins) return fail(ctx, PG_ERR_ARG, "need n_sys >= 1 systems and bins");
-    if (form == PG_FORM_ONEHOT)
-        return fail(ctx, PG_ERR_UNSUPPORTED, "batched runs use the histogram form (the faster form at 50 bins)");
-    if (form != PG_FORM_AUTO && form != PG_FORM_HIST) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
+    if (form < PG_FORM_AUTO || form > PG_FORM_ONEHOT) return fail(ctx, PG_ERR_ARG, "unknown form %d", form);
     for (int k = 0; k < 6; k++) {
         if (bins[k] < 1) return fail(ctx, PG_ERR_ARG, "bin count %d (index %d) < 1", bins[k], k);
         if (k >= 3 && bins[k] > PG_MAX_BINS_2D)
@@ -1360,13 +1363,14 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     cudaStream_t st = ctx->stream;
     ctx->resident = false;
 
-    // Where the autotuner picks the one-hot form for every system (up to 15
-    // bins, long enough trajectories), that form is the faster one even
-    // without a batched launch: the systems run one after another through
-    // pg_entropy + pg_mist on this context, with the same outputs.
-    if (form == PG_FORM_AUTO) {
-        bool onehot = true;
-        for (int s = 0; s < n_sys && onehot; s++) {
+    // The form of the batch: one form for every system, in one pair launch.
+    // Automatically the one-hot form where the autotuner picks it for every
+    // system (the batched one-hot launch runs every system's tiles together).
+    bool onehot = form == PG_FORM_ONEHOT;
+    {
+        bool all_supported = true;
+        std::vector<SysGeom> geos((size_t)n_sys);
+        for (int s = 0; s < n_sys; s++) {
             int rc = validate_view(ctx, &trajs[s], s);
             if (rc) return rc;
             SysGeom g{};
@@ -1377,27 +1381,12 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
             g.D = g.nb + g.na + g.nd;
             g.F = trajs[s].n_frames;
             for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
-            onehot = autotune_form(g) == PG_FORM_ONEHOT;
+            all_supported = all_supported && pairs_onehot_supported(g);
+            geos[s] = g;
         }
-        if (onehot) {
-            for (int s = 0; s < n_sys; s++) {
-                int rc = pg_entropy(ctx, &trajs[s], bins, PG_FORM_ONEHOT, outs ? &outs[s] : nullptr);
-                if (rc) return rc;
-                if (edges || totals) {
-                    const int D = 3 * trajs[s].n_dihedrals + 3;
-                    std::vector<pg_mist_edge> e_tmp;
-                    double t_tmp[10];
-                    pg_mist_edge *e = edges ? edges[s] : nullptr;
-                    if (!e) {
-                        e_tmp.resize((size_t)std::max(D - 1, 1));
-                        e = e_tmp.data();
-                    }
-                    rc = pg_mist(ctx, trajs[s].n_dihedrals, nullptr, e, totals ? totals + 10 * (size_t)s : t_tmp);
-                    if (rc) return rc;
-                }
-            }
-            return PG_OK;
-        }
+        if (form == PG_FORM_ONEHOT && !all_supported)
+            return fail(ctx, PG_ERR_UNSUPPORTED, "one-hot tensor-core form unsupported for a system of the batch");
+        if (form == PG_FORM_AUTO) onehot = autotune_batch_form(geos) == PG_FORM_ONEHOT;
     }
 
     // ---- layout of every system inside one arena
@@ -1418,7 +1407,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         g.F = v.n_frames;
         g.ldb = bins_ld(g.F);
         for (int k = 0; k < 6; k++) g.bins[k] = bins[k];
-        set_bin_layout(g, PG_FORM_HIST);
+        set_bin_layout(g, onehot ? PG_FORM_ONEHOT : PG_FORM_HIST);
         L.prec = v.double_prec;
         L.own_cols = !v.on_device;
         L.ld = v.on_device ? v.ld : v.n_frames;
@@ -1498,10 +1487,14 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     for (int s = 0; s < n_sys; s++) order[s] = s;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sys[a].g.F > sys[b].g.F; });
     for (int s : order) {
+        if (onehot) break;  // the one-hot launch builds its own tile list
         std::vector<PairTile> t = h32 ? build_tiles32(sys[s].g.D) : build_tiles(sys[s].g.D, T);
         tiles.insert(tiles.end(), t.begin(), t.end());
         tsys.insert(tsys.end(), t.size(), s);
     }
+    std::vector<SysGeom> gs((size_t)n_sys);
+    for (int s = 0; s < n_sys; s++) gs[s] = sys[s].g;
+    if (onehot) CK(ctx->ohbatch.ensure(pairs_onehot_batch_bytes(gs)));
     // preprocessing of all systems in one launch per input precision: CTA
     // k handles DOF map[k].y of system map[k].x
     std::vector<PrepDesc> pd((size_t)n_sys);
@@ -1550,6 +1543,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     key.push_back(h32 ? (int64_t)(uintptr_t)ctx->scratch.p : -1);
     key.push_back(sys[0].g.codes);
     key.push_back(sys[0].g.ilv);
+    key.push_back(onehot ? (int64_t)(uintptr_t)ctx->ohbatch.p : -1);
     for (int k = 0; k < 6; k++) key.push_back(bins[k]);
     for (int s = 0; s < n_sys; s++) {
         const pg_bat_view &v = trajs[s];
@@ -1573,6 +1567,19 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
                 CK(cudaMemcpyAsync(meta + (q ? mo_m1 : mo_m0), pmap[q].data(), sizeof(int2) * pmap[q].size(),
                                    cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));  // host vectors go out of scope
+        if (onehot) {
+            // descriptors, row tables and n ln n tables of the one-hot launch
+            std::vector<const uint8_t *> bp((size_t)n_sys);
+            std::vector<DofArrays> dp((size_t)n_sys);
+            std::vector<PairOut> op((size_t)n_sys);
+            for (int s = 0; s < n_sys; s++) {
+                bp[s] = sd[s].bins;
+                dp[s] = sd[s].dof;
+                op[s] = sd[s].out;
+            }
+            CK(prepare_pairs_onehot_batch(gs, bp, dp, op, ctx->ohbatch.p, ctx->ohbatch.n, st));
+            ctx->launches += n_sys;  // one n ln n table per system
+        }
     }
     // host columns -> arena (outside the graph: their source is the caller's)
     for (int s = 0; s < n_sys; s++) {
@@ -1610,7 +1617,10 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
             e = cudaMemcpyAsync(arena + L.par, dofs_at(L).s1, (size_t)L.g.D * sizeof(double), cudaMemcpyDeviceToDevice,
                                 st);
         }
-        if (e == cudaSuccess)
+        int oh_launches = 0;
+        if (e == cudaSuccess && onehot)
+            e = launch_pairs_onehot_batch(gs, ctx->ohbatch.p, (int *)ctx->errw.p, st, &oh_launches);
+        else if (e == cudaSuccess)
             e = h32 ? launch_pairs_hist32_batch(bmax, sys[0].g.codes != 0, sys[0].g.ilv != 0,
                                                 (const SysDesc *)(meta + mo_sd),
                                                 (const PairTile *)(meta + mo_t),
@@ -1633,7 +1643,8 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         ctx->graph_key = key;
     }
     CK(cudaGraphLaunch(ctx->graph, st));
-    ctx->launches += (pmap[0].empty() ? 0 : 1) + (pmap[1].empty() ? 0 : 1) + 2;  // preps, pairs, MIST
+    // preps, pair kernel (+ the one-hot finalize), MIST
+    ctx->launches += (pmap[0].empty() ? 0 : 1) + (pmap[1].empty() ? 0 : 1) + (onehot ? 3 : 2);
     CK(cudaEventRecord(ctx->ev[2], st));
     int rc = check_err_words(ctx);
     float ms[2];
@@ -1645,7 +1656,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     ctx->timings[3] = ms[0];
     ctx->timings[4] = ms[0] + ms[1];
     if (rc) return rc;
-    ctx->last_form = PG_FORM_HIST;
+    ctx->last_form = onehot ? PG_FORM_ONEHOT : PG_FORM_HIST;
 
     // ---- results to the caller
     for (int s = 0; s < n_sys; s++) {

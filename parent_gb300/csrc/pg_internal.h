@@ -239,6 +239,32 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
                                 void *scratch, size_t scratch_bytes, int *launches);
 size_t pairs_onehot_scratch_bytes(const SysGeom &g);
 bool pairs_onehot_supported(const SysGeom &g);
+// launch_pairs_onehot in two parts: the set-up (synchronous uploads, the
+// n ln n table) and the run (accumulators zeroed, pair kernel, finalize),
+// which can be repeated on the same inputs (the autotuner's probes time it).
+struct OnehotRun {
+    void *scratch = nullptr;
+    size_t off_sys = 0, off_fin = 0, off_tiles = 0, off_snl = 0, acc_bytes = 0;
+    int64_t n_tiles = 0;
+    bool pair = true;
+    int D = 0;
+};
+cudaError_t onehot_setup(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, PairOut out, cudaStream_t st,
+                         void *scratch, size_t scratch_bytes, OnehotRun *run);
+cudaError_t onehot_run(const OnehotRun &run, int *err, cudaStream_t st);
+// Many systems in one one-hot launch (each tile names its system; tiles of
+// the longest trajectories first): workspace size, tile count, the set-up
+// of the descriptors and tables that depend only on the geometries
+// (synchronous, outside any graph capture), and the launch itself (zeroes
+// the accumulators, pair kernel, one finalize launch over all systems;
+// capturable).
+size_t pairs_onehot_batch_bytes(const std::vector<SysGeom> &gs);
+int64_t pairs_onehot_batch_tiles(const std::vector<SysGeom> &gs);
+cudaError_t prepare_pairs_onehot_batch(const std::vector<SysGeom> &gs, const std::vector<const uint8_t *> &bins,
+                                       const std::vector<DofArrays> &dofs, const std::vector<PairOut> &outs,
+                                       void *ws, size_t ws_bytes, cudaStream_t st);
+cudaError_t launch_pairs_onehot_batch(const std::vector<SysGeom> &gs, void *ws, int *err, cudaStream_t st,
+                                      int *launches);
 
 // One system of a batched MIST launch (one CTA each); scratch holds
 // key[D] | from[D] | pos[D] (mist_scratch_bytes(D)).
@@ -256,5 +282,20 @@ cudaError_t launch_mi_from_par(int n_dih, const double *par, ParLayout L, double
                                cudaStream_t st);
 
 std::vector<PairTile> build_tiles32(int D);
+// tile count of the one-hot form for a geometry (CTA-pair tiles unless
+// PG_ONEHOT_PAIR=0)
+int64_t pairs_onehot_tiles(const SysGeom &g);
+
+// Histogram layouts: the 16-slot kernel (two lanes per pair), the 32-slot
+// kernel fed by a TMA ring, and the streamed 32-slot kernel (rows loaded
+// straight from the frame-group interleaved bin matrix).
+enum { HIST16 = 0, HIST32_RING = 1, HIST32_STREAM = 2 };
+int hist_layout(const SysGeom &g);
+// The autotuner (pg_autotune.cu): predicted pair-kernel seconds of a form on
+// this GPU (< 0 if unknown), and the form PG_FORM_AUTO takes for one system
+// and for a batch run in one launch.
+double predict_pair_seconds(const SysGeom &g, int form);
+int autotune_form(const SysGeom &g);
+int autotune_batch_form(const std::vector<SysGeom> &gs);
 
 }  // namespace pg

@@ -210,8 +210,23 @@ __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// A tile: row tile (x128, or x256 for a CTA pair) and column tile (x512) of
+// the C of system `sys` of the launch.
 struct TcTile {
-    int mt, nt;  // row tile (x128) and column tile (x512) of C
+    int mt, nt, sys, pad;
+};
+
+// One system of a launch, as the kernel reads it (a single-system launch
+// has one). rowinfo: (dof << 8) | bin for each row of the system's C; nfix:
+// its fixed-point n ln n table; acc_snl/acc_occ: its D x D pair accumulators.
+struct OhSys {
+    const uint8_t *bins;
+    int64_t ldb;
+    const uint32_t *rowinfo;
+    const int64_t *nfix;
+    unsigned long long *acc_snl;
+    unsigned int *acc_occ;
+    int F, R, D, pad;
 };
 
 // Per (row, chunk) item of the one-hot build, fixed for the whole K loop.
@@ -234,11 +249,7 @@ struct Item {
 // MMAs arrives on the "empty" barrier of both CTAs.
 template <bool PAIR>
 __global__ void __launch_bounds__(kThreads, 1)
-onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
-              const uint32_t *__restrict__ rowinfo,  // (dof << 8) | bin for each row of C
-              const TcTile *__restrict__ tiles, const int64_t *__restrict__ nlogn_fix,
-              unsigned long long *__restrict__ acc_snl, unsigned int *__restrict__ acc_occ, int D,
-              int *err) {
+onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tiles, int *err) {
     using C = OhCfg<PAIR>;
     constexpr int kStages = C::kStages, kStageBytes = C::kStageBytes, kBRows = C::kBRows;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -257,6 +268,14 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t rank = PAIR ? cluster_rank() : 0u;
     const TcTile tile = tiles[PAIR ? blockIdx.x >> 1 : blockIdx.x];
+    const OhSys sy = systems[tile.sys];  // both CTAs of a pair read the same tile, so the same system
+    const uint8_t *__restrict__ bins = sy.bins;
+    const int64_t ldb = sy.ldb;
+    const uint32_t *__restrict__ rowinfo = sy.rowinfo;
+    const int64_t *__restrict__ nlogn_fix = sy.nfix;
+    unsigned long long *__restrict__ acc_snl = sy.acc_snl;
+    unsigned int *__restrict__ acc_occ = sy.acc_occ;
+    const int F = sy.F, R = sy.R, D = sy.D;
     const int r0 = PAIR ? tile.mt * 2 * kM + (int)rank * kM : tile.mt * kM;  // this CTA's A rows
     const int c0 = tile.nt * kN;
     const int b0 = PAIR ? c0 + (int)rank * (kNH / 2) : c0;  // first C column of this CTA's B rows
@@ -563,12 +582,28 @@ onehot_kernel(const uint8_t *__restrict__ bins, int64_t ldb, int F, int R,
 
 // S2D and MI of every pair from the accumulators (the histogram kernel's
 // epilogue formula): S = ln N + A_i + A_j - (1/N) sum n ln n + (occ-1)/(2N).
-__global__ void onehot_finalize(SysGeom geo, DofArrays dof, const unsigned long long *acc_snl,
-                                const unsigned int *acc_occ, PairOut out, double lnN, double fix) {
+// One system per blockIdx.z.
+struct OhFin {
+    SysGeom geo;
+    DofArrays dof;
+    const unsigned long long *acc_snl;
+    const unsigned int *acc_occ;
+    PairOut out;
+    double lnN, fix;
+};
+
+__global__ void onehot_finalize(const OhFin *__restrict__ fins) {
+    const OhFin &fn = fins[blockIdx.z];
+    const SysGeom &geo = fn.geo;
+    const DofArrays &dof = fn.dof;
+    const unsigned long long *acc_snl = fn.acc_snl;
+    const unsigned int *acc_occ = fn.acc_occ;
+    const PairOut &out = fn.out;
+    const double lnN = fn.lnN, fix = fn.fix;
     const int D = geo.D;
     const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
     const int g1 = blockIdx.y;
-    if (g2 >= D || g2 <= g1) return;
+    if (g1 >= D || g2 >= D || g2 <= g1) return;
     const int64_t pi = (int64_t)g1 * D + g2;
     const double N = (double)geo.F;
     const double s = (double)acc_snl[pi] / fix;
@@ -582,25 +617,32 @@ __global__ void onehot_finalize(SysGeom geo, DofArrays dof, const unsigned long 
     }
 }
 
-__global__ void rowinfo_kernel(const int *b2, int D, const int64_t *rowstart, uint32_t *rowinfo) {
-    const int g = blockIdx.x;
-    for (int b = threadIdx.x; b < b2[g]; b += blockDim.x) rowinfo[rowstart[g] + b] = ((uint32_t)g << 8) | (uint32_t)b;
-}
 
 
 
 }  // namespace
 
-// Host-side geometry of one launch: rows of C, the tile list and the scratch layout.
+// Host-side geometry of one system: rows of C, its tile list and the
+// scratch layout of a single-system launch.
 struct OnehotPlan {
     int64_t R = 0, n_tiles = 0;
-    size_t off_rowstart = 0, off_rowinfo = 0, off_tiles = 0, off_fix = 0, off_snl = 0, off_occ = 0, total = 0;
+    size_t off_rowstart = 0, off_rowinfo = 0, off_tiles = 0, off_fix = 0, off_snl = 0, off_occ = 0, off_sys = 0,
+           off_fin = 0, total = 0;
 };
 
 static int bins_of(const SysGeom &g, int gd) { return g.bins[3 + dof_type(gd, g.nb, g.na)]; }
+static size_t al256(size_t x) { return (x + 255) / 256 * 256; }
 
-// pair: tiles of 256 rows (a CTA pair each), else 128
-static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles, bool pair = false) {
+// rowinfo of every row of C: (dof << 8) | bin
+static std::vector<uint32_t> rowinfo_of(const SysGeom &g) {
+    std::vector<uint32_t> ri;
+    for (int d = 0; d < g.D; d++)
+        for (int b = 0; b < bins_of(g, d); b++) ri.push_back(((uint32_t)d << 8) | (uint32_t)b);
+    return ri;
+}
+
+// pair: tiles of 256 rows (a CTA pair each), else 128; tiles tagged `sys`
+static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles, bool pair = false, int sys = 0) {
     OnehotPlan p;
     std::vector<int64_t> rs((size_t)g.D + 1, 0);
     for (int d = 0; d < g.D; d++) rs[d + 1] = rs[d] + bins_of(g, d);
@@ -616,20 +658,20 @@ static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles, bool pair =
         for (int64_t nt = 0; nt < nts; nt++) {
             const int64_t cend = std::min(p.R, (nt + 1) * kN) - 1;
             if (dof_at(cend) <= rdof0) continue;  // no pair g1 < g2 in this tile
-            if (tiles) tiles->push_back(TcTile{(int)mt, (int)nt});
+            if (tiles) tiles->push_back(TcTile{(int)mt, (int)nt, sys, 0});
             cnt++;
         }
     }
     p.n_tiles = cnt;
-    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
     p.off_rowstart = 0;
-    p.off_rowinfo = al(p.off_rowstart + sizeof(int64_t) * (g.D + 1));
-    p.off_tiles = al(p.off_rowinfo + sizeof(uint32_t) * (size_t)p.R);
-    p.off_fix = al(p.off_tiles + sizeof(TcTile) * (size_t)cnt);
-    p.off_snl = al(p.off_fix + sizeof(int64_t) * ((size_t)g.F + 1));
-    p.off_occ = al(p.off_snl + sizeof(unsigned long long) * (size_t)g.D * g.D);
-    p.total = al(p.off_occ + sizeof(unsigned int) * (size_t)g.D * g.D);
-    (void)rs;
+    p.off_rowinfo = al256(p.off_rowstart + sizeof(int64_t) * (g.D + 1));
+    p.off_tiles = al256(p.off_rowinfo + sizeof(uint32_t) * (size_t)p.R);
+    p.off_fix = al256(p.off_tiles + sizeof(TcTile) * (size_t)cnt);
+    p.off_snl = al256(p.off_fix + sizeof(int64_t) * ((size_t)g.F + 1));
+    p.off_occ = al256(p.off_snl + sizeof(unsigned long long) * (size_t)g.D * g.D);
+    p.off_sys = al256(p.off_occ + sizeof(unsigned int) * (size_t)g.D * g.D);
+    p.off_fin = al256(p.off_sys + sizeof(OhSys));
+    p.total = al256(p.off_fin + sizeof(OhFin));
     return p;
 }
 
@@ -650,42 +692,18 @@ static bool use_pairs() {
     return !(e && atoi(e) == 0);
 }
 
-cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
-                                const double *, PairOut out, int *err, cudaStream_t st, void *scratch,
-                                size_t scratch_bytes, int *launches) {
-    *launches = 0;
-    if (!pairs_onehot_supported(g)) return cudaErrorInvalidValue;
-    const bool pair = use_pairs();
-    std::vector<TcTile> tiles;
-    const OnehotPlan p = plan(g, &tiles, pair);
-    if (scratch_bytes < p.total) return cudaErrorInvalidValue;
-    char *base = (char *)scratch;
-    std::vector<int64_t> rs((size_t)g.D + 1, 0);
-    for (int d = 0; d < g.D; d++) rs[d + 1] = rs[d] + bins_of(g, d);
-    int64_t *d_rs = (int64_t *)(base + p.off_rowstart);
-    uint32_t *d_ri = (uint32_t *)(base + p.off_rowinfo);
-    TcTile *d_tiles = (TcTile *)(base + p.off_tiles);
-    int64_t *d_fix = (int64_t *)(base + p.off_fix);
-    unsigned long long *d_snl = (unsigned long long *)(base + p.off_snl);
-    unsigned int *d_occ = (unsigned int *)(base + p.off_occ);
+// The pair kernel over a tile list (each tile names its system) and the
+// finalize kernel over n_fin systems (largest D max_D).
+static cudaError_t launch_tiles(const OhSys *d_sys, const TcTile *d_tiles, int64_t n_tiles, bool pair,
+                                const OhFin *d_fin, int n_fin, int max_D, int *err, cudaStream_t st) {
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(d_rs, rs.data(), rs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st))) return e;
-    if ((e = cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice, st)))
-        return e;
-    // the host vectors must outlive the copies
-    if ((e = cudaStreamSynchronize(st))) return e;
-    if ((e = cudaMemsetAsync(d_snl, 0, sizeof(unsigned long long) * (size_t)g.D * g.D, st))) return e;
-    if ((e = cudaMemsetAsync(d_occ, 0, sizeof(unsigned int) * (size_t)g.D * g.D, st))) return e;
-    rowinfo_kernel<<<g.D, 64, 0, st>>>(dof.b2, g.D, d_rs, d_ri);
-    const double fix = nlogn_fix_scale(g.F);  // per-bin rounding error 2^-(s+1)
-    if ((e = launch_nlogn_fix_table((unsigned long long *)d_fix, g.F, fix, st))) return e;
-    if (p.n_tiles > 0) {
+    if (n_tiles > 0) {
         if (pair) {
             const size_t smem = (size_t)OhCfg<true>::kSmemBytes;
             if ((e = cudaFuncSetAttribute(onehot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
                 return e;
             cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3((unsigned)(2 * p.n_tiles));
+            cfg.gridDim = dim3((unsigned)(2 * n_tiles));
             cfg.blockDim = dim3(kThreads);
             cfg.dynamicSmemBytes = smem;
             cfg.stream = st;
@@ -696,36 +714,186 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
             at[0].val.clusterDim.z = 1;
             cfg.attrs = at;
             cfg.numAttrs = 1;
-            if ((e = cudaLaunchKernelEx(&cfg, onehot_kernel<true>, bins, g.ldb, g.F, (int)p.R, (const uint32_t *)d_ri,
-                                        (const TcTile *)d_tiles, (const int64_t *)d_fix, d_snl, d_occ, g.D, err)))
-                return e;
+            if ((e = cudaLaunchKernelEx(&cfg, onehot_kernel<true>, d_sys, d_tiles, err))) return e;
         } else {
             const size_t smem = (size_t)OhCfg<false>::kSmemBytes;
             if ((e = cudaFuncSetAttribute(onehot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem)))
                 return e;
-            onehot_kernel<false><<<(unsigned)p.n_tiles, kThreads, smem, st>>>(bins, g.ldb, g.F, (int)p.R, d_ri,
-                                                                              d_tiles, d_fix, d_snl, d_occ, g.D, err);
+            onehot_kernel<false><<<(unsigned)n_tiles, kThreads, smem, st>>>(d_sys, d_tiles, err);
         }
     }
-    dim3 fg((g.D + 255) / 256, g.D);
-    onehot_finalize<<<fg, 256, 0, st>>>(g, dof, d_snl, d_occ, out, log((double)g.F), fix);
-    *launches = 4;
+    dim3 fg((max_D + 255) / 256, max_D, n_fin);
+    onehot_finalize<<<fg, 256, 0, st>>>(d_fin);
     return cudaGetLastError();
 }
 
-// Form choice, from measured GB300 pair-kernel times at 2,994 DOFs x 100,000
-// frames: the histogram form takes 85.8 ms at any bin count up to 32 (32-slot
-// layout, one conflict-free shared-memory reduction per update) and 117.6 ms
-// from 36 to 50 (16-slot layout); the one-hot form on CTA pairs takes 24.4 /
-// 31.9 / 38.2 / 47.0 / 54.8 / 65.1 / 72.9 / 84.7 / 94.4 ms at 8 .. 16 bins
-// (B1*B2 FP8 MACs per update, so its time grows as B^2). The one-hot form
-// wins up to 15 bins.
-int autotune_form(const SysGeom &g) {
-    int bmax = 0;
-    for (int t = 0; t < 3; t++) bmax = bmax > g.bins[3 + t] ? bmax : g.bins[3 + t];
-    if (pairs_onehot_supported(g) && bmax <= 15 && g.F >= 4096) return PG_FORM_ONEHOT;
-    return PG_FORM_HIST;
+// Single-system launch in two parts: the set-up (uploads of the row table,
+// tiles and descriptors, which the host must wait for, and the n ln n table)
+// and the run (zeroed accumulators, pair kernel, finalize), which can be
+// repeated on the same inputs.
+cudaError_t onehot_setup(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, PairOut out, cudaStream_t st,
+                         void *scratch, size_t scratch_bytes, OnehotRun *run) {
+    if (!pairs_onehot_supported(g)) return cudaErrorInvalidValue;
+    const bool pair = use_pairs();
+    std::vector<TcTile> tiles;
+    const OnehotPlan p = plan(g, &tiles, pair);
+    if (scratch_bytes < p.total) return cudaErrorInvalidValue;
+    char *base = (char *)scratch;
+    const std::vector<uint32_t> ri = rowinfo_of(g);
+    uint32_t *d_ri = (uint32_t *)(base + p.off_rowinfo);
+    TcTile *d_tiles = (TcTile *)(base + p.off_tiles);
+    int64_t *d_fix = (int64_t *)(base + p.off_fix);
+    unsigned long long *d_snl = (unsigned long long *)(base + p.off_snl);
+    unsigned int *d_occ = (unsigned int *)(base + p.off_occ);
+    const double fix = nlogn_fix_scale(g.F);  // per-bin rounding error 2^-(s+1)
+    const OhSys hs{bins, g.ldb, d_ri, d_fix, d_snl, d_occ, g.F, (int)p.R, g.D, 0};
+    const OhFin hf{g, dof, d_snl, d_occ, out, log((double)g.F), fix};
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_ri, ri.data(), ri.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice, st)))
+        return e;
+    if ((e = cudaMemcpyAsync(base + p.off_sys, &hs, sizeof hs, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(base + p.off_fin, &hf, sizeof hf, cudaMemcpyHostToDevice, st))) return e;
+    // the host copies must outlive the transfers
+    if ((e = cudaStreamSynchronize(st))) return e;
+    if ((e = launch_nlogn_fix_table((unsigned long long *)d_fix, g.F, fix, st))) return e;
+    run->scratch = scratch;
+    run->off_sys = p.off_sys;
+    run->off_fin = p.off_fin;
+    run->off_tiles = p.off_tiles;
+    run->off_snl = p.off_snl;
+    run->acc_bytes = p.off_sys - p.off_snl;  // the accumulators up to the descriptors
+    run->n_tiles = p.n_tiles;
+    run->pair = pair;
+    run->D = g.D;
+    return cudaSuccess;
 }
+
+cudaError_t onehot_run(const OnehotRun &run, int *err, cudaStream_t st) {
+    char *base = (char *)run.scratch;
+    cudaError_t e = cudaMemsetAsync(base + run.off_snl, 0, run.acc_bytes, st);
+    if (e != cudaSuccess) return e;
+    return launch_tiles((const OhSys *)(base + run.off_sys), (const TcTile *)(base + run.off_tiles), run.n_tiles,
+                        run.pair, (const OhFin *)(base + run.off_fin), 1, run.D, err, st);
+}
+
+cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
+                                const double *, PairOut out, int *err, cudaStream_t st, void *scratch,
+                                size_t scratch_bytes, int *launches) {
+    *launches = 0;
+    OnehotRun run;
+    cudaError_t e = onehot_setup(g, bins, dof, out, st, scratch, scratch_bytes, &run);
+    if (e != cudaSuccess) return e;
+    *launches = 3;  // n ln n table, pair kernel, finalize
+    return onehot_run(run, err, st);
+}
+
+// ---- many systems in one launch (pg_entropy_batch)
+//
+// Workspace: OhSys[n] | OhFin[n] | tiles | per system: rowinfo, n ln n table
+// | the accumulators of all systems, contiguous (one memset per run).
+struct OhBatchLayout {
+    std::vector<size_t> off_ri, off_fix, off_snl, off_occ;
+    size_t off_sys = 0, off_fin = 0, off_tiles = 0, acc_begin = 0, acc_end = 0, total = 0;
+    std::vector<TcTile> tiles;
+    int max_D = 1;
+};
+
+static OhBatchLayout batch_layout(const std::vector<SysGeom> &gs, bool pair) {
+    OhBatchLayout L;
+    const int n = (int)gs.size();
+    // tiles of the systems with the most frames (the longest tiles) first
+    std::vector<int> order((size_t)n);
+    for (int s = 0; s < n; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return gs[a].F > gs[b].F; });
+    for (int s : order) plan(gs[s], &L.tiles, pair, s);
+    size_t off = 0;
+    L.off_sys = off;
+    off = al256(off + sizeof(OhSys) * n);
+    L.off_fin = off;
+    off = al256(off + sizeof(OhFin) * n);
+    L.off_tiles = off;
+    off = al256(off + sizeof(TcTile) * std::max<size_t>(L.tiles.size(), 1));
+    L.off_ri.resize(n);
+    L.off_fix.resize(n);
+    L.off_snl.resize(n);
+    L.off_occ.resize(n);
+    for (int s = 0; s < n; s++) {
+        int64_t R = 0;
+        for (int d = 0; d < gs[s].D; d++) R += bins_of(gs[s], d);
+        L.off_ri[s] = off;
+        off = al256(off + sizeof(uint32_t) * (size_t)R);
+        L.off_fix[s] = off;
+        off = al256(off + sizeof(int64_t) * ((size_t)gs[s].F + 1));
+        L.max_D = std::max(L.max_D, gs[s].D);
+    }
+    L.acc_begin = off;
+    for (int s = 0; s < n; s++) {
+        L.off_snl[s] = off;
+        off += sizeof(unsigned long long) * (size_t)gs[s].D * gs[s].D;
+        L.off_occ[s] = off;
+        off = (off + sizeof(unsigned int) * (size_t)gs[s].D * gs[s].D + 7) / 8 * 8;
+    }
+    L.acc_end = off;
+    L.total = al256(off);
+    return L;
+}
+
+size_t pairs_onehot_batch_bytes(const std::vector<SysGeom> &gs) { return batch_layout(gs, use_pairs()).total; }
+
+int64_t pairs_onehot_batch_tiles(const std::vector<SysGeom> &gs) {
+    return (int64_t)batch_layout(gs, use_pairs()).tiles.size();
+}
+
+cudaError_t prepare_pairs_onehot_batch(const std::vector<SysGeom> &gs, const std::vector<const uint8_t *> &bins,
+                                       const std::vector<DofArrays> &dofs, const std::vector<PairOut> &outs,
+                                       void *ws, size_t ws_bytes, cudaStream_t st) {
+    const bool pair = use_pairs();
+    const OhBatchLayout L = batch_layout(gs, pair);
+    if (ws_bytes < L.total) return cudaErrorInvalidValue;
+    const int n = (int)gs.size();
+    char *base = (char *)ws;
+    std::vector<OhSys> hs((size_t)n);
+    std::vector<OhFin> hf((size_t)n);
+    std::vector<std::vector<uint32_t>> ri((size_t)n);
+    cudaError_t e;
+    for (int s = 0; s < n; s++) {
+        const SysGeom &g = gs[s];
+        if (!pairs_onehot_supported(g)) return cudaErrorInvalidValue;
+        ri[s] = rowinfo_of(g);
+        const double fix = nlogn_fix_scale(g.F);
+        hs[s] = OhSys{bins[s], g.ldb, (const uint32_t *)(base + L.off_ri[s]), (const int64_t *)(base + L.off_fix[s]),
+                      (unsigned long long *)(base + L.off_snl[s]), (unsigned int *)(base + L.off_occ[s]), g.F,
+                      (int)ri[s].size(), g.D, 0};
+        hf[s] = OhFin{g, dofs[s], hs[s].acc_snl, hs[s].acc_occ, outs[s], log((double)g.F), fix};
+        if ((e = cudaMemcpyAsync(base + L.off_ri[s], ri[s].data(), ri[s].size() * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, st)))
+            return e;
+        if ((e = launch_nlogn_fix_table((unsigned long long *)(base + L.off_fix[s]), g.F, fix, st))) return e;
+    }
+    if ((e = cudaMemcpyAsync(base + L.off_sys, hs.data(), sizeof(OhSys) * n, cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(base + L.off_fin, hf.data(), sizeof(OhFin) * n, cudaMemcpyHostToDevice, st))) return e;
+    if (!L.tiles.empty() &&
+        (e = cudaMemcpyAsync(base + L.off_tiles, L.tiles.data(), sizeof(TcTile) * L.tiles.size(),
+                             cudaMemcpyHostToDevice, st)))
+        return e;
+    return cudaStreamSynchronize(st);  // the host vectors go out of scope
+}
+
+cudaError_t launch_pairs_onehot_batch(const std::vector<SysGeom> &gs, void *ws, int *err, cudaStream_t st,
+                                      int *launches) {
+    const bool pair = use_pairs();
+    const OhBatchLayout L = batch_layout(gs, pair);
+    char *base = (char *)ws;
+    cudaError_t e = cudaMemsetAsync(base + L.acc_begin, 0, L.acc_end - L.acc_begin, st);
+    if (e != cudaSuccess) return e;
+    *launches = 2;
+    return launch_tiles((const OhSys *)(base + L.off_sys), (const TcTile *)(base + L.off_tiles),
+                        (int64_t)L.tiles.size(), pair, (const OhFin *)(base + L.off_fin), (int)gs.size(), L.max_D,
+                        err, st);
+}
+
+int64_t pairs_onehot_tiles(const SysGeom &g) { return plan(g, nullptr, use_pairs()).n_tiles; }
 
 }  // namespace pg

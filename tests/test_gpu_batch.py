@@ -72,8 +72,9 @@ def test_batch_both_histogram_layouts_at_50_bins(eng, monkeypatch, slots):
 
 def test_batch_at_10_bins_takes_the_onehot_form(eng):
     """At 10 bins the autotuner picks the one-hot form for every system with
-    at least 4,096 frames: the batch runs them one by one through that form;
-    bodies and trees equal the oracle's and the single one-hot calls'."""
+    at least 4,096 frames: the batch runs every system's tiles in one
+    tensor-core launch; bodies and trees equal the oracle's and the single
+    one-hot calls' (bit for bit: each system keeps its own n ln n table)."""
     bins = (10,) * 6
     spec = [(40, 12345, 0), (25, 5000, 1), (60, 20000, 0), (17, 4096, 0)]
     trajs = _systems(spec, seed0=31)
@@ -81,6 +82,25 @@ def test_batch_at_10_bins_takes_the_onehot_form(eng):
     assert eng.last_form() == "onehot"
     _check_against_oracle(trajs, bodies, trees, bins)
     for t, b, (e, tot) in zip(trajs, bodies, trees):
+        single = eng.entropy(t, bins, "onehot")
+        assert np.array_equal(b.flat(), single.flat())
+
+
+@pytest.mark.parametrize("pair", ["1", "0"])
+def test_batch_onehot_form_on_ragged_systems(eng, monkeypatch, pair):
+    """The batched one-hot launch forced on ragged systems (no dihedrals, one
+    frame, FP64 and FP32, per-type bin counts), on CTA pairs and on single
+    CTAs: the oracle's bodies and trees, the single calls' bodies bit for
+    bit, and a replayed graph gives the same results."""
+    monkeypatch.setenv("PG_ONEHOT_PAIR", pair)
+    bins = (10, 12, 9, 10, 12, 9)
+    trajs = _systems(SYSTEMS, seed0=91)
+    bodies, trees = eng.entropy_batch(trajs, bins, form="onehot")
+    assert eng.last_form() == "onehot"
+    _check_against_oracle(trajs, bodies, trees, bins)
+    again = eng.entropy_batch(trajs, bins, form="onehot")
+    for t, b, b2 in zip(trajs, bodies, again[0]):
+        assert np.array_equal(b.flat(), b2.flat())
         single = eng.entropy(t, bins, "onehot")
         assert np.array_equal(b.flat(), single.flat())
 
@@ -156,8 +176,8 @@ def test_batch_outputs_optional(eng):
 
 def test_batch_errors(eng):
     t = _systems([(10, 1000, 1)])[0]
-    with pytest.raises(pg.PGError) as ex:
-        eng.entropy_batch([t], (50,) * 6, form="onehot")
+    with pytest.raises(pg.PGError) as ex:   # the one-hot form needs 8..127 bins
+        eng.entropy_batch([t], (50, 50, 50, 50, 4, 50), form="onehot")
     assert ex.value.code == pg.PG_ERR_UNSUPPORTED
     with pytest.raises(pg.PGError) as ex:
         eng.entropy_batch([t], (50, 50, 50, 50, 50, 0))

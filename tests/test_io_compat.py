@@ -179,3 +179,19 @@ def test_reference_post_processors_link_against_this_library(tmp_path, prog, ste
         assert r.returncode == 0, r.stderr[-2000:]
         got = r.stdout
     assert got == want
+
+
+def test_library_exports_every_io_function_declared():
+    """Every function include/parent_gb300_io.h declares is defined in the
+    library with that C++ signature (nm demangles the exported names)."""
+    import re
+    hdr = (INCLUDE / "parent_gb300_io.h").read_text()
+    names = re.findall(r"PG_IO_API\s+int\s+(\w+)\s*\(", hdr)
+    assert len(names) == 8
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm is not installed")
+    out = subprocess.run([nm, "-D", "--defined-only", "-C", str(LIBDIR / "libparent_gb300.so")],
+                         capture_output=True, text=True, check=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}\(std::basic_[io]fstream", out), n
