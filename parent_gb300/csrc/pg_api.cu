@@ -392,9 +392,28 @@ static std::vector<PairTile> layout_tiles(const SysGeom &g, int *T_out) {
     *T_out = h32 ? 32 : T;
     return h32 ? build_tiles32(g.D) : build_tiles(g.D, T);
 }
-static void shard_range(int64_t n, int shard, int n_shards, int64_t *b, int64_t *e) {
-    *b = n * shard / n_shards;
-    *e = n * (shard + 1) / n_shards;
+// The contiguous tile range [b, e) of shard `shard`: cut where the running
+// work passes shard / n_shards of the total, a tile's work being its pair
+// slots with r < c (the counting, which dominates) plus two for streaming its
+// bin rows, so shards of diagonal and ragged-edge tiles take more tiles.
+static void shard_range(const std::vector<PairTile> &tl, int shard, int n_shards, int64_t *b, int64_t *e) {
+    std::vector<double> cum(tl.size() + 1, 0.0);
+    for (size_t k = 0; k < tl.size(); k++) {
+        const PairTile &t = tl[k];
+        int pairs = 0;
+        for (int r = 0; r < t.nrow; r++)
+            for (int c = 0; c < t.ncol; c++) pairs += t.row0 + r < t.col0 + c;
+        cum[k + 1] = cum[k] + pairs + 2.0;
+    }
+    const double W = cum.back();
+    auto cut = [&](int s) -> int64_t {
+        if (s <= 0) return 0;
+        if (s >= n_shards) return (int64_t)tl.size();
+        const double target = W * s / n_shards;
+        return (int64_t)(std::lower_bound(cum.begin(), cum.end(), target) - cum.begin());
+    };
+    *b = cut(shard);
+    *e = std::max(*b, cut(shard + 1));
 }
 
 // Entropies of a HOST trajectory, the upload optionally overlapped: the DOFs
@@ -948,7 +967,7 @@ PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_sh
     memset(mask, 0, (size_t)L.total);
     if (shard == 0) memset(mask, 1, (size_t)g.D);  // the 1D entropies (body offsets 0 .. D-1)
     int64_t b = 0, e = 0;
-    shard_range((int64_t)tl.size(), shard, n_shards, &b, &e);
+    shard_range(tl, shard, n_shards, &b, &e);
     for (int64_t k = b; k < e; k++) {
         const PairTile &t = tl[k];
         for (int r = 0; r < t.nrow; r++)
@@ -983,7 +1002,7 @@ PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins
     const std::vector<PairTile> tl = layout_tiles(g, &T);
     if (tl.empty() && g.D > 1) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
     int64_t b = 0, e = 0;
-    shard_range((int64_t)tl.size(), shard, n_shards, &b, &e);
+    shard_range(tl, shard, n_shards, &b, &e);
     PairOut po;
     po.par = (double *)ctx->par.p;
     po.mi = nullptr;  // a shard's MI matrix is partial: MIST runs on the merged body

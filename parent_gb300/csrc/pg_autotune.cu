@@ -102,12 +102,11 @@ cudaError_t make_probe(Probe &p, const SysGeom &like, int D, int F, cudaStream_t
     // every DOF's bins below its own 2D bin count, at the positions the
     // layout puts them (DOF rows ldb apart, or frame-group interleaved)
     std::vector<uint8_t> h(nbins, 0);
-    const int64_t Dp = ilv_dp(g.D);
     for (int d = 0; d < g.D; d++) {
         const uint64_t B = (uint64_t)g.bins[3 + dof_type(d, g.nb, g.na)];
         for (int f = 0; f < F; f++) {
             const uint64_t r = mix(((uint64_t)d << 32) ^ (uint64_t)f);
-            const int64_t at = g.ilv ? ilv_index(Dp, d, f) : (int64_t)d * g.ldb + f;
+            const int64_t at = g.ilv ? ilv_index(F, d, f) : (int64_t)d * g.ldb + f;
             h[(size_t)at] = (uint8_t)(r % B);
         }
     }

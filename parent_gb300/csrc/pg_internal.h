@@ -35,17 +35,24 @@ struct SysGeom {
 };
 
 // Frame-group interleaved bin layout (SysGeom::ilv), read by the streamed
-// 32-slot histogram kernel: frames in groups of 16, group k holds the 16
-// bytes of every DOF, DOF g at byte (k * ilv_dp(D) + g) * 16, so the bins
-// of consecutive DOFs for one group are contiguous (a tile's 4 row DOFs are
-// 64 bytes, its 8 column DOFs one 128-byte line). D is padded to a multiple
-// of 8 so that every group and every 8-DOF column block starts on a line.
+// 32-slot histogram kernel. Frames go in groups of 16 and DOFs in blocks of
+// 8; block k holds, for every group in frame order, the 16 bytes of each of
+// its 8 DOFs (128 bytes per group): DOF g, frame f at
+//   ((g / 8) * G + f / 16) * 128 + (g % 8) * 16 + f % 16,  G = ilv_groups(F).
+// A tile's 8 column DOFs (a block) are then one 128-byte line per group and
+// its 4 row DOFs half of one, and consecutive groups of a DOF are 128 bytes
+// apart, so a warp streams its groups at small constant offsets. D is padded
+// to a multiple of 8.
 __host__ __device__ inline int64_t ilv_dp(int D) { return ((int64_t)D + 7) / 8 * 8; }
 __host__ __device__ inline int64_t ilv_groups(int F) { return ((int64_t)F + 15) / 16; }
 __host__ __device__ inline int64_t ilv_bytes(int D, int F) { return ilv_groups(F) * ilv_dp(D) * 16; }
-__host__ __device__ inline int64_t ilv_index(int64_t Dp, int g, int f) {
-    return ((int64_t)(f >> 4) * Dp + g) * 16 + (f & 15);
+// byte offset of DOF g's first group
+__host__ __device__ inline int64_t ilv_dof_base(int F, int g) {
+    return (int64_t)(g >> 3) * ilv_groups(F) * 128 + (g & 7) * 16;
 }
+// byte offset of (DOF g, frame f) from that base
+__host__ __device__ inline int64_t ilv_frame_off(int f) { return ((int64_t)(f >> 4) << 7) + (f & 15); }
+__host__ __device__ inline int64_t ilv_index(int F, int g, int f) { return ilv_dof_base(F, g) + ilv_frame_off(f); }
 
 // Bytes of the bin matrix (and the row-code matrix after it, if any).
 inline size_t bins_bytes(const SysGeom &g) {

@@ -425,17 +425,17 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
 // ---------------------------------------------------------------------------
 // Streamed form of the same layouts. The TMA ring above makes every consumer
 // warp wait on, and release, every chunk of the tile: each warp only counts
-// fc/31 frames of a chunk, so the per-chunk synchronisation and the uneven
-// split of a chunk's 16-frame groups over 31 warps are paid for every few
+// fc/31 frames of a chunk, so the per-chunk synchronisation is paid every few
 // hundred updates, and beside 160 KB of 16-bit counters only two 2,048-frame
-// stages fit. Here there is no ring: all 32 warps count, each streams its
-// own 16-frame groups (group k goes to warp k mod 32) straight from global
-// memory into registers, two groups ahead, from the frame-group interleaved
-// bin layout (ilv_index), in which one group of a tile's 4 row DOFs is 64
-// contiguous bytes and of its 8 column DOFs one 128-byte line, so a warp's
-// two 16-byte loads per group touch two lines. The warps meet only at the
-// end of a tile (and at the 16-bit folds). Counting, folds and the epilogue
-// are those of the ring kernel.
+// stages fit. Here there is no ring: all 32 warps count, each streams its own
+// 16-frame groups (group k goes to warp k mod 32) straight from global memory
+// into registers from the frame-group interleaved bin layout (ilv_index), in
+// which a tile's 8 column DOFs are one 128-byte line per group, its 4 row
+// DOFs half of one, and a warp's consecutive groups are 4 KB apart: three
+// register buffers rotate, so every load is issued two groups before its
+// bytes are counted, at constant offsets from one pointer per operand. The
+// warps meet only at the end of a tile (and at the 16-bit folds). Counting,
+// folds and the epilogue are those of the ring kernel.
 constexpr int kFoldGroups = kFoldFrames / 16;
 
 // 16 bytes from global memory, not kept in L1 (each line is read once)
@@ -523,7 +523,6 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid
         const PairTile tile = a.tiles[t];
         const int F = d.geo.F, D = d.geo.D;
         const int G = (F + 15) >> 4, Gfull = F >> 4;
-        const int64_t gstride = ilv_dp(D) * 16;
         const int gr = pr < tile.nrow ? tile.row0 + pr : -1;
         const int gc = pc < tile.ncol ? tile.col0 + pc : -1;
         const bool valid = gr >= 0 && gc >= 0 && gr < gc;
@@ -533,48 +532,64 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid
         const bool risky = valid && (W32 ? false : d.dof.m2[gc] > 65535);
         const bool folding = !W32 && __any_sync(0xffffffffu, risky) && G > kFoldGroups;
         // rows: bins (32-bit counters) or row codes (16-bit), after the bins
-        const uint8_t *rp = (W32 ? d.bins : d.bins + ilv_bytes(D, F)) + (int64_t)(valid ? gr : 0) * 16;
-        const uint8_t *cp = d.bins + (int64_t)(valid ? gc : 0) * 16;
+        const uint8_t *rbase = (W32 ? d.bins : d.bins + ilv_bytes(D, F)) + ilv_dof_base(F, valid ? gr : 0);
+        const uint8_t *cbase = d.bins + ilv_dof_base(F, valid ? gc : 0);
+        constexpr int kStep = 32 * 128;  // bytes from one of a warp's groups to its next
         const int span = folding ? kFoldGroups : G;
         for (int g0 = 0; g0 < G; g0 += span) {
             const int gend = min(G, g0 + span);
             const int fe = min(gend, Gfull);  // whole groups of this span end here
             if (valid) {
-                int g = g0 + warp;
-                uint4 r0 = make_uint4(0u, 0u, 0u, 0u), c0 = r0, r1 = r0, c1 = r0;
-                if (g < fe) {
-                    r0 = ldg_stream(rp + (int64_t)g * gstride);
-                    c0 = ldg_stream(cp + (int64_t)g * gstride);
+                // this warp's whole groups of the span: g0 + warp + 32 k, k < nk
+                const int first = g0 + warp;
+                const int nk = fe > first ? (fe - first + 31) / 32 : 0;
+                const uint8_t *rp = rbase + (int64_t)first * 128;
+                const uint8_t *cp = cbase + (int64_t)first * 128;
+                uint4 ar = make_uint4(0u, 0u, 0u, 0u), ac = ar, br = ar, bc = ar, cr = ar, cc = ar;
+                if (nk > 0) {
+                    ar = ldg_stream(rp);
+                    ac = ldg_stream(cp);
                 }
-                if (g + 32 < fe) {
-                    r1 = ldg_stream(rp + (int64_t)(g + 32) * gstride);
-                    c1 = ldg_stream(cp + (int64_t)(g + 32) * gstride);
+                if (nk > 1) {
+                    br = ldg_stream(rp + kStep);
+                    bc = ldg_stream(cp + kStep);
                 }
-                for (; g < fe; g += 32) {
-                    const uint4 r = r0, c = c0;
-                    r0 = r1;
-                    c0 = c1;
-                    if (g + 64 < fe) {
-                        r1 = ldg_stream(rp + (int64_t)(g + 64) * gstride);
-                        c1 = ldg_stream(cp + (int64_t)(g + 64) * gstride);
+                int k = 0;
+                for (; k + 2 < nk; k += 3) {
+                    cr = ldg_stream(rp + 2 * kStep);
+                    cc = ldg_stream(cp + 2 * kStep);
+                    count_group<W32>(ar, ac, Bc, hbase, a.kw, a.kneg);
+                    if (k + 3 < nk) {
+                        ar = ldg_stream(rp + 3 * kStep);
+                        ac = ldg_stream(cp + 3 * kStep);
                     }
-                    count_group<W32>(r, c, Bc, hbase, a.kw, a.kneg);
+                    count_group<W32>(br, bc, Bc, hbase, a.kw, a.kneg);
+                    if (k + 4 < nk) {
+                        br = ldg_stream(rp + 4 * kStep);
+                        bc = ldg_stream(cp + 4 * kStep);
+                    }
+                    count_group<W32>(cr, cc, Bc, hbase, a.kw, a.kneg);
+                    rp += 3 * kStep;
+                    cp += 3 * kStep;
                 }
+                if (k < nk) count_group<W32>(ar, ac, Bc, hbase, a.kw, a.kneg);
+                if (k + 1 < nk) count_group<W32>(br, bc, Bc, hbase, a.kw, a.kneg);
                 // the ragged last group of the trajectory, on the warp whose
                 // turn it is
                 if (Gfull < gend && Gfull >= g0 && ((Gfull - g0) & 31) == warp) {
-                    const uint4 rv = ldg_stream(rp + (int64_t)Gfull * gstride);
-                    const uint4 cv = ldg_stream(cp + (int64_t)Gfull * gstride);
+                    const uint4 rv = ldg_stream(rbase + (int64_t)Gfull * 128);
+                    const uint4 cv = ldg_stream(cbase + (int64_t)Gfull * 128);
                     const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
                     const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
                     const int n = F - Gfull * 16;
 #pragma unroll
-                    for (int k = 0; k < 16; k++) {
-                        if (k < n) {
-                            const uint32_t br = (rw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                            const uint32_t bc = (cw[k >> 2] >> (8 * (k & 3))) & 0xffu;
-                            if (W32) red_add1_nc(hbase + ((br * Bc + bc) << 7));
-                            else red_add_nc(hbase + (((br & 0x7fu) * Bc + bc) << 7), (br & 0x80u) ? 0xFFFF0001u : 1u);
+                    for (int q = 0; q < 16; q++) {
+                        if (q < n) {
+                            const uint32_t brow = (rw[q >> 2] >> (8 * (q & 3))) & 0xffu;
+                            const uint32_t bcol = (cw[q >> 2] >> (8 * (q & 3))) & 0xffu;
+                            if (W32) red_add1_nc(hbase + ((brow * Bc + bcol) << 7));
+                            else red_add_nc(hbase + (((brow & 0x7fu) * Bc + bcol) << 7),
+                                            (brow & 0x80u) ? 0xFFFF0001u : 1u);
                         }
                     }
                 }

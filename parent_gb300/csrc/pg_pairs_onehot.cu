@@ -73,8 +73,9 @@ struct OhCfg {
     static constexpr int kBStage = kBRows * kKB;
     static constexpr int kStageBytes = kAStage + kBStage;
     // byte offsets inside the dynamic shared memory
-    static constexpr int kOffBar = kStages * kStageBytes;  // full[kStages] | empty[kStages] | binfull[kBinBufs]
-    static constexpr int kNumBars = 2 * kStages + kBinBufs;
+    // full[kStages] | empty[kStages] | binfull[kBinBufs] | drained
+    static constexpr int kOffBar = kStages * kStageBytes;
+    static constexpr int kNumBars = 2 * kStages + kBinBufs + 1;
     static constexpr int kOffTmem = kOffBar + kNumBars * 8;
     static constexpr int kOffPsSnl = (kOffTmem + 16 + 15) / 16 * 16;
     static constexpr int kOffPsOcc = kOffPsSnl + kMaxRowDofs * kMaxColDofs * 8;
@@ -83,6 +84,14 @@ struct OhCfg {
     static_assert(kSmemBytes <= 227 * 1024, "one-hot kernel shared memory");
 };
 constexpr long long kWaitCycles = 4000000000LL;
+// Frames per accumulation chunk: the FP32 accumulators hold 4 x the count of
+// one chunk (exact below 2^24); at the end of every chunk but the last, the
+// counts are moved into INT32 totals in global memory (one 128 x 512 slot per
+// SM: one CTA of this kernel per SM at a time) and the accumulators restart.
+constexpr int kChunkFrames = 1 << 20;
+constexpr int kChunkKB = kChunkFrames / 128;   // K-blocks per chunk
+constexpr int kDrainWarps = 4;                 // warps 0..3, one per TMEM lane quarter
+constexpr size_t kDrainSlotWords = 128 * 512;
 // Fixed-point scale of n ln n: the largest power of two 2^s (s <= 44) with
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -226,7 +235,8 @@ struct OhSys {
     const int64_t *nfix;
     unsigned long long *acc_snl;
     unsigned int *acc_occ;
-    int F, R, D, pad;
+    uint32_t *drain;  // INT32 totals of trajectories longer than a chunk: [slot][512 cols][128 rows]
+    int F, R, D, drain_slots;
 };
 
 // Per (row, chunk) item of the one-hot build, fixed for the whole K loop.
@@ -257,6 +267,7 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
     uint64_t *full = (uint64_t *)(smem + C::kOffBar);  // stage built (one arrival per builder warp, both CTAs)
     uint64_t *empty = full + kStages;                  // stage's MMAs done (tcgen05.commit)
     uint64_t *binfull = empty + kStages;               // K-block bin rows stored (one arrival per builder warp)
+    uint64_t *drained = binfull + C::kBinBufs;         // a chunk's accumulators moved to the INT32 totals
     uint32_t *tmem_slot = (uint32_t *)(smem + C::kOffTmem);
     unsigned long long *ps_snl = (unsigned long long *)(smem + C::kOffPsSnl);  // [kMaxRowDofs][kMaxColDofs]
     unsigned int *ps_occ = (unsigned int *)(smem + C::kOffPsOcc);
@@ -302,6 +313,8 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
             mbar_init(smem_u32(&empty[k]), 1);
         }
         for (int k = 0; k < C::kBinBufs; k++) mbar_init(smem_u32(&binfull[k]), kBuilderWarps);
+        // the drain warps of both CTAs of a pair arrive on the first CTA's barrier
+        mbar_init(smem_u32(drained), (PAIR ? 2 : 1) * kDrainWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_r0dof = (int)(rowinfo[r0 < R ? r0 : R - 1] >> 8);
         s_c0dof = (int)(rowinfo[c0 < R ? c0 : R - 1] >> 8);
@@ -323,6 +336,15 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
     const int blast = (int)(rowinfo[min(b0 + (PAIR ? kN - kNH / 2 : kN), R) - 1] >> 8);  // last B row's DOF
     const int nkb = (F + kKB - 1) / kKB;
     unsigned char *binbuf = smem + C::kOffBins;  // [C::kBinBufs][kBinSlots][kKB]
+    // INT32 totals of this SM's slot (trajectories longer than one chunk)
+    const bool chunked = nkb > kChunkKB;
+    uint32_t smid = 0;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    uint32_t *totals = (chunked && sy.drain && (int)smid < sy.drain_slots) ? sy.drain + (size_t)smid * kDrainSlotWords
+                                                                          : nullptr;
+    if (chunked && !totals) {  // no drain area for this SM: report, count nothing
+        if (tid == 0) atomicAdd(&err[ERR_TIMEOUT], 1);
+    }
 
     if (warp == kLoaderWarp) {
         // ------------------------------------------------------- MMA issuer
@@ -338,10 +360,21 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
                              ? 1
                              : 0;
                 ok = __shfl_sync(0xffffffffu, ok, 0);
-                if (!ok || s_abort) {
+                if (ok && chunked && kb % kChunkKB == 0) {
+                    // the previous chunk's accumulators are in the INT32 totals
+                    // (both CTAs of a pair) before this chunk's MMAs restart them
+                    if (lane == 0)
+                        ok = (PAIR ? mbar_wait_cluster_bounded(smem_u32(drained), (uint32_t)((kb / kChunkKB - 1) & 1))
+                                   : mbar_wait_bounded(smem_u32(drained), (uint32_t)((kb / kChunkKB - 1) & 1)))
+                                 ? 1
+                                 : 0;
+                    ok = __shfl_sync(0xffffffffu, ok, 0);
+                }
+                if (!ok || s_abort || (chunked && !totals)) {
                     if (lane == 0) s_abort = 1;
                     break;
                 }
+                const int kc = kb % kChunkKB;  // K-block inside its chunk: 0 restarts the accumulators
                 if (lane == 0) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t a0 = sbase + s * kStageBytes, bb0 = a0 + kAStage;
@@ -351,8 +384,8 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
                         for (int h = 0; h < kN / kNH; h++) {  // B rows of MMA h start kBRows/2 rows further
                             const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
                             const uint64_t bd = smem_desc(bb0 + h * (kBRows / 2 / 8) * 1024 + kk * 256, 128, 1024);
-                            if (PAIR) mma_f8_pair(tmem + h * kNH, ad, bd, (kb | kk) != 0);
-                            else mma_f8(tmem + h * kNH, ad, bd, (kb | kk) != 0);
+                            if (PAIR) mma_f8_pair(tmem + h * kNH, ad, bd, (kc | kk) != 0);
+                            else mma_f8(tmem + h * kNH, ad, bd, (kc | kk) != 0);
                         }
                     }
                     if (PAIR) mma_commit_pair(smem_u32(&empty[s]));
@@ -484,6 +517,42 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&full[s]));
             if (kb + 2 < nkb) store_block(kb + 2, pf, pv);
+            if (chunked && warp < kDrainWarps && (kb + 1) % kChunkKB == 0 && kb + 1 < nkb) {
+                // end of a chunk: once its MMAs are done (the commit of this
+                // block), move this warp's TMEM lane quarter into the totals
+                if (!totals ||
+                    !mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)((kb / kStages) & 1))) {
+                    s_abort = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const bool first = kb + 1 == kChunkKB;
+                const int row = 32 * warp + lane;
+                for (int ch = 0; ch < kN / 16; ch++) {
+                    uint32_t v[16];
+                    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(ch * 16);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                          "=r"(v[15])
+                        : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const uint32_t n = __float2uint_rn(__uint_as_float(v[q])) >> 2;  // 2.0 x 2.0 per frame
+                        uint32_t *t = totals + (size_t)(ch * 16 + q) * 128 + row;
+                        *t = first ? n : *t + n;
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __threadfence_block();
+                __syncwarp();
+                if (lane == 0) {
+                    if (PAIR && rank != 0) mbar_arrive_cluster(map_to_rank(smem_u32(drained), 0u));
+                    else mbar_arrive(smem_u32(drained));
+                }
+            }
         }
     }
     __syncthreads();
@@ -552,7 +621,8 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
             if (cdof < 0) break;        // past the last row of C
             if (cdof <= rdof) continue;  // only pairs g1 < g2
             if (cdof != cur) flush(cdof);
-            const unsigned int n = (unsigned int)__float2uint_rn(__uint_as_float(v[q])) >> 2;  // 2.0 x 2.0 per frame
+            unsigned int n = (unsigned int)__float2uint_rn(__uint_as_float(v[q])) >> 2;  // 2.0 x 2.0 per frame
+            if (chunked) n += totals[(size_t)(cbase + ch * 16 + q) * 128 + row];  // earlier chunks
             if (n) {
                 snl += (unsigned long long)__ldg(nlogn_fix + n);
                 occ++;
@@ -620,15 +690,45 @@ __global__ void onehot_finalize(const OhFin *__restrict__ fins) {
 
 
 
+__global__ void nsmid_kernel(int *out) {
+    uint32_t n;
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(n));
+    *out = (int)n;
+}
+
 }  // namespace
+
+// Number of SM ids of the current device (%nsmid: the ids need not be
+// contiguous, so this bounds them), looked up once per device: the INT32
+// totals of chunked one-hot runs have one slot per id.
+static int device_nsmid() {
+    static int cache[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && cache[dev] > 0) return cache[dev];
+    int n = 0, *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) == cudaSuccess) {
+        nsmid_kernel<<<1, 1>>>(d);
+        if (cudaMemcpy(&n, d, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) n = 0;
+        cudaFree(d);
+    }
+    cudaGetLastError();
+    if (n <= 0) cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (dev >= 0 && dev < 64) cache[dev] = n;
+    return n;
+}
 
 // Host-side geometry of one system: rows of C, its tile list and the
 // scratch layout of a single-system launch.
 struct OnehotPlan {
     int64_t R = 0, n_tiles = 0;
     size_t off_rowstart = 0, off_rowinfo = 0, off_tiles = 0, off_fix = 0, off_snl = 0, off_occ = 0, off_sys = 0,
-           off_fin = 0, total = 0;
+           off_fin = 0, off_drain = 0, total = 0;
+    int drain_slots = 0;
 };
+
+// INT32 totals: one slot per SM id when the trajectory is longer than a chunk
+static int drain_slots_for(int F) { return F > kChunkFrames ? device_nsmid() : 0; }
 
 static int bins_of(const SysGeom &g, int gd) { return g.bins[3 + dof_type(gd, g.nb, g.na)]; }
 static size_t al256(size_t x) { return (x + 255) / 256 * 256; }
@@ -671,7 +771,9 @@ static OnehotPlan plan(const SysGeom &g, std::vector<TcTile> *tiles, bool pair =
     p.off_occ = al256(p.off_snl + sizeof(unsigned long long) * (size_t)g.D * g.D);
     p.off_sys = al256(p.off_occ + sizeof(unsigned int) * (size_t)g.D * g.D);
     p.off_fin = al256(p.off_sys + sizeof(OhSys));
-    p.total = al256(p.off_fin + sizeof(OhFin));
+    p.off_drain = al256(p.off_fin + sizeof(OhFin));
+    p.drain_slots = drain_slots_for(g.F);
+    p.total = al256(p.off_drain + sizeof(uint32_t) * kDrainSlotWords * (size_t)p.drain_slots);
     return p;
 }
 
@@ -679,7 +781,7 @@ bool pairs_onehot_supported(const SysGeom &g) {
     for (int t = 0; t < 3; t++)
         if (g.bins[3 + t] < 8 || g.bins[3 + t] > 127) return false;  // per-tile DOF tables sized for >= 8 bins;
                                                                      // bin bytes below 128 for the one-hot build
-    return g.F < (1 << 22);  // FP32 accumulators hold 4 x count, exact below 2^24
+    return g.F >= 1;  // longer than one chunk (2^20 frames): INT32 totals across chunks
 }
 
 size_t pairs_onehot_scratch_bytes(const SysGeom &g) { return plan(g, nullptr).total; }
@@ -747,7 +849,8 @@ cudaError_t onehot_setup(const SysGeom &g, const uint8_t *bins, const DofArrays 
     unsigned long long *d_snl = (unsigned long long *)(base + p.off_snl);
     unsigned int *d_occ = (unsigned int *)(base + p.off_occ);
     const double fix = nlogn_fix_scale(g.F);  // per-bin rounding error 2^-(s+1)
-    const OhSys hs{bins, g.ldb, d_ri, d_fix, d_snl, d_occ, g.F, (int)p.R, g.D, 0};
+    const OhSys hs{bins, g.ldb, d_ri, d_fix, d_snl, d_occ,
+                   p.drain_slots ? (uint32_t *)(base + p.off_drain) : nullptr, g.F, (int)p.R, g.D, p.drain_slots};
     const OhFin hf{g, dof, d_snl, d_occ, out, log((double)g.F), fix};
     cudaError_t e;
     if ((e = cudaMemcpyAsync(d_ri, ri.data(), ri.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st))) return e;
@@ -795,9 +898,9 @@ cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const Dof
 // | the accumulators of all systems, contiguous (one memset per run).
 struct OhBatchLayout {
     std::vector<size_t> off_ri, off_fix, off_snl, off_occ;
-    size_t off_sys = 0, off_fin = 0, off_tiles = 0, acc_begin = 0, acc_end = 0, total = 0;
+    size_t off_sys = 0, off_fin = 0, off_tiles = 0, acc_begin = 0, acc_end = 0, off_drain = 0, total = 0;
     std::vector<TcTile> tiles;
-    int max_D = 1;
+    int max_D = 1, drain_slots = 0;
 };
 
 static OhBatchLayout batch_layout(const std::vector<SysGeom> &gs, bool pair) {
@@ -836,7 +939,11 @@ static OhBatchLayout batch_layout(const std::vector<SysGeom> &gs, bool pair) {
         off = (off + sizeof(unsigned int) * (size_t)gs[s].D * gs[s].D + 7) / 8 * 8;
     }
     L.acc_end = off;
-    L.total = al256(off);
+    int maxF = 0;
+    for (const SysGeom &g : gs) maxF = std::max(maxF, g.F);
+    L.drain_slots = drain_slots_for(maxF);
+    L.off_drain = al256(off);
+    L.total = al256(L.off_drain + sizeof(uint32_t) * kDrainSlotWords * (size_t)L.drain_slots);
     return L;
 }
 
@@ -864,8 +971,9 @@ cudaError_t prepare_pairs_onehot_batch(const std::vector<SysGeom> &gs, const std
         ri[s] = rowinfo_of(g);
         const double fix = nlogn_fix_scale(g.F);
         hs[s] = OhSys{bins[s], g.ldb, (const uint32_t *)(base + L.off_ri[s]), (const int64_t *)(base + L.off_fix[s]),
-                      (unsigned long long *)(base + L.off_snl[s]), (unsigned int *)(base + L.off_occ[s]), g.F,
-                      (int)ri[s].size(), g.D, 0};
+                      (unsigned long long *)(base + L.off_snl[s]), (unsigned int *)(base + L.off_occ[s]),
+                      L.drain_slots ? (uint32_t *)(base + L.off_drain) : nullptr, g.F, (int)ri[s].size(), g.D,
+                      L.drain_slots};
         hf[s] = OhFin{g, dofs[s], hs[s].acc_snl, hs[s].acc_occ, outs[s], log((double)g.F), fix};
         if ((e = cudaMemcpyAsync(base + L.off_ri[s], ri[s].data(), ri[s].size() * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, st)))

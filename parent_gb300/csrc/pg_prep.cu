@@ -277,11 +277,10 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
     // DOF rows ldb bytes apart, or the frame-group interleaved layout
     // (ilv_index) of the streamed 32-slot histogram kernel
-    const int64_t Dp = ilv_dp(geo.D);
-    uint8_t *brow = geo.ilv ? bins + (int64_t)g * 16 : bins + (int64_t)g * geo.ldb;
+    uint8_t *brow = geo.ilv ? bins + ilv_dof_base(F, g) : bins + (int64_t)g * geo.ldb;
     // row codes for the 16-bit 32-slot histogram layouts: (b >> 1) | (b & 1) << 7
     uint8_t *crow = !geo.codes ? nullptr
-                    : (geo.ilv ? bins + ilv_bytes(geo.D, F) + (int64_t)g * 16
+                    : (geo.ilv ? bins + ilv_bytes(geo.D, F) + ilv_dof_base(F, g)
                                : bins + ((int64_t)geo.D + g) * geo.ldb);
     int bad = 0;
     {
@@ -324,7 +323,7 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
             atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
-            const int64_t at = geo.ilv ? ((int64_t)(f >> 4) * Dp) * 16 + (f & 15) : (int64_t)f;
+            const int64_t at = geo.ilv ? ilv_frame_off(f) : (int64_t)f;
             brow[at] = (uint8_t)i2;
             if (crow) crow[at] = (uint8_t)((i2 >> 1) | ((i2 & 1) << 7));
         }

@@ -190,6 +190,26 @@ def test_onehot_form_matches_oracle(eng, monkeypatch, n_atoms, F, prec, bins, pa
     compare_mist(e, tot, re, rt)
 
 
+@pytest.mark.parametrize("n_atoms,F,bins", [
+    (10, 1_300_000, (10,) * 6),          # two 2^20-frame chunks: one move into the INT32 totals
+    (8, 4_500_000, (12, 9, 16, 12, 9, 16)),  # five chunks, past the FP32 accumulators' 2^22-frame limit
+])
+@pytest.mark.parametrize("pair", ["1", "0"])
+def test_onehot_counts_accumulate_over_frame_chunks(eng, monkeypatch, n_atoms, F, bins, pair):
+    """Trajectories longer than one 2^20-frame chunk: at each chunk end the
+    tensor memory's FP32 counts are moved into INT32 totals and the
+    accumulators restart, so the form has no frame limit. Same values as the
+    oracle and as the histogram form."""
+    monkeypatch.setenv("PG_ONEHOT_PAIR", pair)
+    t = _synth_case(n_atoms, F, 0, seed=F + n_atoms, frac_bimodal_dih=0.3, frac_bimodal_bond=0.1)
+    body = eng.entropy(t, bins, "onehot")
+    assert eng.last_form() == "onehot"
+    ref = oracle.parent(t.bonds, t.angles, t.dihedrals, bins)
+    compare_bodies(n_atoms - 3, body, ref)
+    hist = eng.entropy(t, bins, "hist")
+    assert np.max(np.abs(hist.flat() - body.flat())) <= 1e-12
+
+
 def test_onehot_and_hist_agree_on_fixture(eng):
     bat = pg.BatFile(GOLDEN / "ubq_sub.bat")
     a = eng.entropy(bat.view(), (50,) * 6, "onehot").flat()

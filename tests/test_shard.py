@@ -32,9 +32,9 @@ def test_shard_masks_partition_the_body(n_dih, bins, n_shards):
     assert owners.min() == 1 and owners.max() == 1
     D = 3 * n_dih + 3
     assert masks[0][:D].all()  # shard 0 owns the 1D entropies
-    if n_shards > 1 and n_dih >= 20:  # pair entries are spread evenly
+    if n_shards > 1 and n_dih >= 20:  # shards are cut by pair work, not tile count
         sizes = [int(m[D:].sum()) for m in masks]
-        assert max(sizes) <= 1.6 * (sum(sizes) / n_shards)
+        assert max(sizes) <= 1.1 * (sum(sizes) / n_shards), sizes
 
 
 def test_shard_mask_rejects_bad_arguments():
