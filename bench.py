@@ -72,12 +72,13 @@ def replica_seed(base: int, rank: int) -> int:
     return base + 7919 * rank
 
 
-def traffic_per_update(slots: int):
+def traffic_per_update(layout: str):
     """DRAM bytes per update of the pair kernel from the committed ncu capture
     (profiles/), or None: the capture is on a smaller case (2,994 DOFs x 100k
     frames) and is scaled by this launch's updates."""
-    name = ("pairs_hist32_kernel_precision_path_2994dof_100k_30bins.md" if slots == 32
-            else "pairs_hist_kernel_precision_path_2994dof_100k.md")
+    name = {"stream32": "pairs_hist32s_kernel_precision_path_2994dof_100k_50bins.md",
+            "ring32": "pairs_hist32_kernel_precision_path_2994dof_100k_30bins.md",
+            "16": "pairs_hist_kernel_precision_path_2994dof_100k.md"}[layout]
     try:
         for line in (ROOT / "profiles" / name).read_text().splitlines():
             if line.startswith("dram_bytes_per_update:"):
@@ -87,13 +88,18 @@ def traffic_per_update(slots: int):
     return None, name
 
 
-def hist_slots(bins: int) -> int:
-    """Pair slots per CTA of the histogram layout the library picks (32 with
-    32-bit counters up to 35 bins, else 16; PG_HIST_SLOTS forces one)."""
+def hist_layout(bins: int) -> str:
+    """The histogram layout the library picks (parent_gb300/csrc/pg_autotune.cu
+    hist_layout): the streamed 32-slot kernel up to 50 bins, else 16 slots;
+    PG_HIST_SLOTS / PG_HIST_STREAM override it."""
     forced = os.environ.get("PG_HIST_SLOTS")
-    if forced in ("16", "32"):
-        return 32 if forced == "32" and bins <= 50 else 16
-    return 32 if bins <= 35 else 16
+    if forced == "16":
+        return "16"
+    if forced == "32":
+        return "ring32" if bins <= 50 else "16"
+    if os.environ.get("PG_HIST_STREAM") == "0":
+        return "ring32" if bins <= 35 else "16"
+    return "stream32" if bins <= 50 else "16"
 
 
 def parse():
@@ -423,7 +429,7 @@ def run_batch(args):
             "config": {"workload": BATCH, "systems": len(systems), "dofs": [min(Ds), max(Ds)],
                        "frames": [min(Fs), max(Fs)], "updates_per_step": units, "input": "fp32",
                        "bins": args.bins, "form": batch_form,
-                       "hist_slots": hist_slots(args.bins) if batch_form == "hist" else None,
+                       "hist_layout": hist_layout(args.bins) if batch_form == "hist" else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (total_bytes / 1e9)},
             "sequential": {"ms_per_step": ms_seq, "value": units * world / (ms_seq / 1e3),
@@ -579,7 +585,7 @@ def run_gb300(args):
     if form == "hist":
         red_peak = eng.probe_smem_red_rate()
         achieved = units / pair_s
-        bpu, prof = traffic_per_update(hist_slots(args.bins))
+        bpu, prof = traffic_per_update(hist_layout(args.bins))
         roofline = {"bound": "smem", "achieved": achieved / 1e9, "peak": red_peak / 1e9, "unit": "Gred/s",
                     "frac": achieved / red_peak, "traffic": bpu * units if bpu else None,
                     "note": "one shared-memory reduction per pair-frame update; peak = conflict-free "
@@ -612,7 +618,7 @@ def run_gb300(args):
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": args.workload, "n_atoms": n_atoms, "dofs": D, "pairs": P, "frames": F,
                        "input": "fp64" if prec else "fp32", "bins": args.bins, "form": form,
-                       "hist_slots": hist_slots(args.bins) if form == "hist" else None,
+                       "hist_layout": hist_layout(args.bins) if form == "hist" else None,
                        "parallelism": f"replicas x{world}" if world > 1 else "single gpu",
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (D * F * es / 1e9)},
             "kernel_ms": {"prep": statistics.mean(prep_ms), "pairs": statistics.mean(pair_ms),

@@ -295,19 +295,21 @@ bool autotune_enabled() {
 
 }  // namespace
 
-// From measured inner-loop rates: the 32-slot ring kernel with 32-bit
-// counters (one wavefront per warp-wide reduction) for 2D bin counts up to
-// 35; the 16-slot kernel above that, where the 32-slot kernels need 16-bit
-// counters. PG_HIST_SLOTS=16 or 32 forces the 16-slot or the 32-slot ring
-// layout (32 slots up to 50 bins); PG_HIST_STREAM=1 the streamed one.
+// The histogram layout, from measured pair-kernel times at 2,994 DOFs x
+// 100,000 frames: the streamed 32-slot kernel up to 50 2D bins (93.0 ms at 50
+// bins against 116.3 ms for the 16-slot kernel and 116.3 ms for the ring-fed
+// 32-slot kernel; 76.9 against 79.7 ms at 30 bins), the 16-slot kernel above
+// (its 32-bit counters reach 218 bins). PG_HIST_SLOTS=16 forces the 16-slot
+// layout, PG_HIST_SLOTS=32 the ring-fed 32-slot one, PG_HIST_STREAM=0 keeps
+// the streamed one off.
 int hist_layout(const SysGeom &g) {
     const int bm = bmax_of(g);
     const char *e = getenv("PG_HIST_SLOTS");
     const char *st = getenv("PG_HIST_STREAM");
     if (e && atoi(e) == 16) return HIST16;
-    if (st && atoi(st) == 1 && pairs_hist32_supported(bm)) return HIST32_STREAM;
     if (e && atoi(e) == 32) return pairs_hist32_supported(bm) ? HIST32_RING : HIST16;
-    return pairs_hist32_wide(bm) ? HIST32_RING : HIST16;
+    if (st && atoi(st) == 0) return pairs_hist32_wide(bm) ? HIST32_RING : HIST16;
+    return pairs_hist32_supported(bm) ? HIST32_STREAM : HIST16;
 }
 
 // Predicted pair-kernel seconds of a geometry in a form (PG_FORM_HIST with

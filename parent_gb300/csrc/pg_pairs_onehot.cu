@@ -520,8 +520,10 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
             if (chunked && warp < kDrainWarps && (kb + 1) % kChunkKB == 0 && kb + 1 < nkb) {
                 // end of a chunk: once its MMAs are done (the commit of this
                 // block), move this warp's TMEM lane quarter into the totals
-                if (!totals ||
-                    !mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)((kb / kStages) & 1))) {
+                int ok = 0;  // lane 0 waits, the warp follows it (the TMEM loads below are warp-wide)
+                if (lane == 0)
+                    ok = totals && mbar_wait_bounded(smem_u32(&empty[s]), (uint32_t)((kb / kStages) & 1)) ? 1 : 0;
+                if (!__shfl_sync(0xffffffffu, ok, 0)) {
                     s_abort = 1;
                     break;
                 }

@@ -22,8 +22,8 @@ pytestmark = pytest.mark.gpu
 
 def _run(n_atoms, frames, bins, form="auto", seed=20261, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05,
          monkeypatch=None, stream=False):
-    if stream:
-        monkeypatch.setenv("PG_HIST_STREAM", "1")
+    if monkeypatch is not None:  # the streamed 32-slot layout (the default) or the ring-fed / 16-slot one
+        monkeypatch.setenv("PG_HIST_STREAM", "1" if stream else "0")
     t = pg.synth_host(n_atoms, frames, double_prec=0, seed=seed, frac_bimodal_dih=frac_bimodal_dih,
                       frac_bimodal_bond=frac_bimodal_bond)
     with pg.Engine(0) as eng:

@@ -288,17 +288,18 @@ def test_mist_over_a_cluster_matches_oracle(eng, monkeypatch, cluster):
     compare_mist(e, tot, re, rt)
 
 
-@pytest.mark.parametrize("groups", ["4", "16", "4-stream"])
+@pytest.mark.parametrize("groups", ["4", "16", "4-ring"])
 def test_grouped_upload_schedule_matches(eng, monkeypatch, groups):
     """PG_STREAM_GROUPS > 1 (uploads in DOF groups on the copy stream, pair
     launches alternating between two streams) gives the same body, bit for
-    bit, as the default one-group upload; also with the streamed 32-slot
-    layout (its integer n ln n sums equal the other layouts' bit for bit)."""
+    bit, as the default one-group upload; also with the ring-fed 32-slot
+    layout instead of the streamed one (their integer n ln n sums are equal
+    bit for bit)."""
     t = _synth_case(150, 6000, 0, seed=23, frac_bimodal_dih=0.2)
     base = eng.entropy(t, (50,) * 6, "hist").flat()
     monkeypatch.setenv("PG_STREAM_GROUPS", groups.split("-")[0])
-    if groups.endswith("stream"):
-        monkeypatch.setenv("PG_HIST_STREAM", "1")
+    if groups.endswith("ring"):
+        monkeypatch.setenv("PG_HIST_STREAM", "0")
     assert np.array_equal(eng.entropy(t, (50,) * 6, "hist").flat(), base)
 
 
