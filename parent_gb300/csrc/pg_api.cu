@@ -335,8 +335,8 @@ static void set_bin_layout(SysGeom &g, int form) {
     if (chosen == PG_FORM_ONEHOT && !pairs_onehot_supported(g)) chosen = PG_FORM_HIST;
     const bool hist = chosen != PG_FORM_ONEHOT;
     const int layout = hist ? hist_layout(g) : HIST16;
-    g.codes = layout != HIST16 && !pairs_hist32_wide(bmax_of(g)) ? 1 : 0;
-    g.ilv = layout == HIST32_STREAM ? 1 : 0;
+    g.codes = layout_codes(layout, bmax_of(g));
+    g.ilv = layout_ilv(layout);
 }
 
 // Launches the 32-slot kernel over the cached full tile list (explicit ==

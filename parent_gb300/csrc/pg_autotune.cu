@@ -106,13 +106,8 @@ cudaError_t make_probe(Probe &p, const SysGeom &like, int D, int F, cudaStream_t
         const uint64_t B = (uint64_t)g.bins[3 + dof_type(d, g.nb, g.na)];
         for (int f = 0; f < F; f++) {
             const uint64_t r = mix(((uint64_t)d << 32) ^ (uint64_t)f);
-            const int64_t at = g.ilv ? ilv_index(F, d, f) : (int64_t)d * g.ldb + f;
-            h[(size_t)at] = (uint8_t)(r % B);
+            store_bin(h.data(), g, d, f, (int)(r % B));
         }
-    }
-    if (g.codes) {  // the row-code matrix after the bins: (b >> 1) | (b & 1) << 7
-        const size_t half = nbins / 2;
-        for (size_t i = 0; i < half; i++) h[half + i] = (uint8_t)((h[i] >> 1) | ((h[i] & 1) << 7));
     }
     if ((e = cudaMemcpyAsync(p.bins, h.data(), nbins, cudaMemcpyHostToDevice, st))) return e;
     double *dd = nullptr;
@@ -273,8 +268,8 @@ TileCost cost_of(const SysGeom &g, int variant) {
 // the bin layout a histogram-form run of g writes and reads
 SysGeom as_hist(const SysGeom &g, int layout) {
     SysGeom h = g;
-    h.codes = layout != HIST16 && !pairs_hist32_wide(bmax_of(g)) ? 1 : 0;
-    h.ilv = layout == HIST32_STREAM ? 1 : 0;
+    h.codes = layout_codes(layout, bmax_of(g));
+    h.ilv = layout_ilv(layout);
     return h;
 }
 SysGeom as_onehot(const SysGeom &g) {
@@ -311,6 +306,9 @@ int hist_layout(const SysGeom &g) {
     if (st && atoi(st) == 0) return pairs_hist32_wide(bm) ? HIST32_RING : HIST16;
     return pairs_hist32_supported(bm) ? HIST32_STREAM : HIST16;
 }
+
+int layout_codes(int layout, int bmax) { return layout != HIST16 && !pairs_hist32_wide(bmax) ? 1 : 0; }
+int layout_ilv(int layout) { return layout == HIST32_STREAM ? 1 : 0; }
 
 // Predicted pair-kernel seconds of a geometry in a form (PG_FORM_HIST with
 // the layout hist_layout picks, or PG_FORM_ONEHOT), or < 0 if unknown.

@@ -60,6 +60,14 @@ inline size_t bins_bytes(const SysGeom &g) {
     return one * (g.codes ? 2 : 1);
 }
 
+// Stores 2D bin b of DOF d, frame f in every matrix of g's layout.
+__host__ __device__ inline void store_bin(uint8_t *bins, const SysGeom &g, int d, int f, int b) {
+    const int64_t at = g.ilv ? ilv_index(g.F, d, f) : (int64_t)d * g.ldb + f;
+    bins[at] = (uint8_t)b;
+    // row codes for the 16-bit 32-slot layouts: (b >> 1) | (b & 1) << 7
+    if (g.codes) bins[(g.ilv ? ilv_bytes(g.D, g.F) : (int64_t)g.D * g.ldb) + at] = (uint8_t)((b >> 1) | ((b & 1) << 7));
+}
+
 __host__ __device__ inline int dof_type(int g, int nb, int na) {
     return g < nb ? TB : (g < nb + na ? TA : TD);
 }
@@ -298,6 +306,9 @@ int64_t pairs_onehot_tiles(const SysGeom &g);
 // straight from the frame-group interleaved bin matrix).
 enum { HIST16 = 0, HIST32_RING = 1, HIST32_STREAM = 2 };
 int hist_layout(const SysGeom &g);
+// SysGeom::codes / SysGeom::ilv of a histogram layout at a bin count
+int layout_codes(int layout, int bmax);
+int layout_ilv(int layout);
 // The autotuner (pg_autotune.cu): predicted pair-kernel seconds of a form on
 // this GPU (< 0 if unknown), and the form PG_FORM_AUTO takes for one system
 // and for a batch run in one launch.

@@ -275,13 +275,6 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const double mn = s_mn, mx = s_mx;
     const double bs1 = __ddiv_rn(__dsub_rn(mx, mn), (double)B1);
     const double bs2 = __ddiv_rn(__dsub_rn(mx, mn), (double)B2);
-    // DOF rows ldb bytes apart, or the frame-group interleaved layout
-    // (ilv_index) of the streamed 32-slot histogram kernel
-    uint8_t *brow = geo.ilv ? bins + ilv_dof_base(F, g) : bins + (int64_t)g * geo.ldb;
-    // row codes for the 16-bit 32-slot histogram layouts: (b >> 1) | (b & 1) << 7
-    uint8_t *crow = !geo.codes ? nullptr
-                    : (geo.ilv ? bins + ilv_bytes(geo.D, F) + ilv_dof_base(F, g)
-                               : bins + ((int64_t)geo.D + g) * geo.ldb);
     int bad = 0;
     {
         // d = fl64(x' - mn) (x' the shifted value for dihedrals) is formed in
@@ -323,9 +316,8 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
             atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
-            const int64_t at = geo.ilv ? ilv_frame_off(f) : (int64_t)f;
-            brow[at] = (uint8_t)i2;
-            if (crow) crow[at] = (uint8_t)((i2 >> 1) | ((i2 & 1) << 7));
+            // every bin matrix of the layout the pair kernel reads
+            store_bin(bins, geo, g, f, i2);
         }
     }
     if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);

@@ -55,9 +55,9 @@ def test_batch_matches_oracle(eng, bins):
 
 @pytest.mark.parametrize("slots", ["16", "32", "stream"])
 def test_batch_both_histogram_layouts_at_50_bins(eng, monkeypatch, slots):
-    """At 50 bins the batch runs the 16-slot layout or, forced, the 32-slot
-    layout with 16-bit counters (row codes written per system), ring-fed or
-    streamed from each system's interleaved bin matrices."""
+    """At 50 bins the batch runs the 32-slot layout with 16-bit counters (row
+    codes written per system), streamed from each system's interleaved bin
+    matrices or ring-fed, or the 16-slot layout."""
     if slots == "stream":
         monkeypatch.setenv("PG_HIST_STREAM", "1")
     else:

@@ -21,9 +21,11 @@ pytestmark = pytest.mark.gpu
 
 
 def _run(n_atoms, frames, bins, form="auto", seed=20261, frac_bimodal_dih=0.2, frac_bimodal_bond=0.05,
-         monkeypatch=None, stream=False):
-    if monkeypatch is not None:  # the streamed 32-slot layout (the default) or the ring-fed / 16-slot one
-        monkeypatch.setenv("PG_HIST_STREAM", "1" if stream else "0")
+         monkeypatch=None, stream="1"):
+    if monkeypatch is not None:
+        # the streamed 32-slot layout (1, the default) or the ring-fed /
+        # 16-slot one (0)
+        monkeypatch.setenv("PG_HIST_STREAM", stream)
     t = pg.synth_host(n_atoms, frames, double_prec=0, seed=seed, frac_bimodal_dih=frac_bimodal_dih,
                       frac_bimodal_bond=frac_bimodal_bond)
     with pg.Engine(0) as eng:
@@ -45,7 +47,7 @@ def _assert_ok(res):
     assert res["mist_max_abs_dMI_nats"] <= 1e-9, res
 
 
-@pytest.mark.parametrize("stream", [False, True])
+@pytest.mark.parametrize("stream", ["0", "1"])
 def test_precision_path_system_matches_oracle_at_50_bins(monkeypatch, stream):
     res, used = _run(1000, 100_000, (50,) * 6, monkeypatch=monkeypatch, stream=stream)
     assert used == "hist"
@@ -53,7 +55,7 @@ def test_precision_path_system_matches_oracle_at_50_bins(monkeypatch, stream):
     _assert_ok(res)
 
 
-@pytest.mark.parametrize("stream", [False, True])
+@pytest.mark.parametrize("stream", ["0", "1"])
 def test_precision_path_system_matches_oracle_at_30_bins(monkeypatch, stream):
     # the 32-slot layout with 32-bit counters, ring-fed or streamed
     res, used = _run(1000, 100_000, (30,) * 6, seed=777, monkeypatch=monkeypatch, stream=stream)

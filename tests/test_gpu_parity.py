@@ -414,8 +414,9 @@ def test_hist32_layout_matches_oracle(eng, monkeypatch, n_atoms, F, bins, feed):
     counters for row-bin pairs above, odd row-bin counts included) gives the
     same counts and values, fed by the TMA ring or streamed from the
     frame-group interleaved bin matrix (ragged last groups included)."""
-    monkeypatch.setenv("PG_HIST_SLOTS", "32")
-    if feed == "stream":
+    if feed == "ring":
+        monkeypatch.setenv("PG_HIST_SLOTS", "32")
+    else:
         monkeypatch.setenv("PG_HIST_STREAM", "1")
     t = _synth_case(n_atoms, F, 0, seed=n_atoms + F, frac_bimodal_dih=0.2)
     body = eng.entropy(t, bins, "hist")

@@ -93,10 +93,11 @@ def test_two_gloo_ranks_merge_shards_exactly():
 @pytest.mark.gpu
 @pytest.mark.parametrize("n_atoms,F,bins,n_shards", [(60, 20000, (50,) * 6, 3), (40, 9000, (30,) * 6, 2),
                                                        (25, 5000, (50, 50, 50, 100, 100, 100), 4)])
-@pytest.mark.parametrize("stream", [False, True])
+@pytest.mark.parametrize("stream", ["0", "1"])
 def test_gpu_shards_sum_to_the_whole(monkeypatch, n_atoms, F, bins, n_shards, stream):
-    # the streamed 32-slot layout where it applies (2D bins <= 50), else the ring-fed or 16-slot one
-    monkeypatch.setenv("PG_HIST_STREAM", "1" if stream else "0")
+    # the streamed 32-slot layout where it applies (2D bins <= 50), else the
+    # ring-fed or 16-slot one
+    monkeypatch.setenv("PG_HIST_STREAM", stream)
     t = pg.synth_host(n_atoms, F, double_prec=0, seed=n_atoms, frac_bimodal_dih=0.2)
     n = n_atoms - 3
     with pg.Engine(0) as eng:
