@@ -68,6 +68,28 @@ __host__ __device__ inline void store_bin(uint8_t *bins, const SysGeom &g, int d
     if (g.codes) bins[(g.ilv ? ilv_bytes(g.D, g.F) : (int64_t)g.D * g.ldb) + at] = (uint8_t)((b >> 1) | ((b & 1) << 7));
 }
 
+// Stores the 2D bins b[0..N) of DOF d, frames f0..f0+N-1 (N = 2 or 4, f0 a
+// multiple of N: the run lies in one DOF row or one 16-frame group, on an
+// N-byte boundary) with one store per matrix.
+template <int N>
+__device__ inline void store_bin_run(uint8_t *bins, const SysGeom &g, int d, int f0, const int *b) {
+    const int64_t at = g.ilv ? ilv_index(g.F, d, f0) : (int64_t)d * g.ldb + f0;
+    uint32_t w = 0, c = 0;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        w |= (uint32_t)b[k] << (8 * k);
+        c |= (uint32_t)((b[k] >> 1) | ((b[k] & 1) << 7)) << (8 * k);
+    }
+    uint8_t *cm = bins + (g.ilv ? ilv_bytes(g.D, g.F) : (int64_t)g.D * g.ldb);
+    if (N == 4) {
+        *(uint32_t *)(bins + at) = w;
+        if (g.codes) *(uint32_t *)(cm + at) = c;
+    } else {
+        *(uint16_t *)(bins + at) = (uint16_t)w;
+        if (g.codes) *(uint16_t *)(cm + at) = (uint16_t)c;
+    }
+}
+
 __host__ __device__ inline int dof_type(int g, int nb, int na) {
     return g < nb ? TB : (g < nb + na ? TA : TD);
 }

@@ -49,11 +49,18 @@ __device__ __forceinline__ int bin_index(double x, double mn, double bs) {
 
 // floor(q) if [q - eps, q + eps] (directed rounding) holds no integer and
 // q - eps >= 0, else -1 (also for NaN).
+// The floors are read off the FP32 adder, not the conversion unit: for
+// 0 <= v < 2^22, fl_rd(v + 2^23) = 2^23 + floor(v) exactly (the spacing of
+// floats in [2^23, 2^24) is 1), whose bits minus those of 2^23 are floor(v).
 __device__ __forceinline__ int screened_floor(float q, float eps) {
     const float lo = __fsub_rd(q, eps), hi = __fadd_ru(q, eps);
-    const int il = __float2int_rd(lo), ih = __float2int_rd(hi);
-    return (lo >= 0.f && il == ih) ? il : -1;
+    const float yl = __fadd_rd(lo, 8388608.f), yh = __fadd_rd(hi, 8388608.f);
+    return (lo >= 0.f && hi < 4194304.f && yl == yh) ? __float_as_int(yl) - 0x4B000000 : -1;
 }
+
+// (float)k for 0 <= k < 2^23, on the adder: the float with bits
+// 0x4B000000 + k is exactly 2^23 + k
+__device__ __forceinline__ float small_int_float(int k) { return __fsub_rn(__int_as_float(0x4B000000 + k), 8388608.f); }
 
 // v ~ hi + lo as two floats (|v - hi - lo| <= 2^-48 |v|)
 struct F2 {
@@ -85,6 +92,92 @@ __device__ __forceinline__ double okey_double(unsigned long long k) {
     const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
     return __longlong_as_double((long long)b);
 }
+
+// The same images for the input type: FP32 values keep 32-bit keys (the
+// conversion to FP64 is exact and monotone, so the same values win; only the
+// winners are converted), FP64 values the keys above.
+template <typename T>
+struct OKey;
+template <>
+struct OKey<float> {
+    using K = unsigned int;
+    static __device__ __forceinline__ K key(float x) {
+        unsigned int b = __float_as_uint(x);
+        if (b == 0x80000000u) b = 0u;
+        return (b >> 31) ? ~b : (b | 0x80000000u);
+    }
+    static __device__ __forceinline__ bool nan(float x) { return (__float_as_uint(x) & 0x7fffffffu) > 0x7f800000u; }
+    static __device__ __forceinline__ double value(unsigned long long k) {
+        const unsigned int c = (unsigned int)k;
+        return (double)__uint_as_float((c >> 31) ? (c & 0x7fffffffu) : ~c);
+    }
+    static constexpr K kNone = 0xffffffffu;
+};
+template <>
+struct OKey<double> {
+    using K = unsigned long long;
+    static __device__ __forceinline__ K key(double x) { return okey_raw(x); }
+    static __device__ __forceinline__ bool nan(double x) { return is_nan_bits(x); }
+    static __device__ __forceinline__ double value(unsigned long long k) { return okey_double(k); }
+    static constexpr K kNone = ~0ull;
+};
+
+// A column is streamed in runs of V = 16 / sizeof(T) consecutive frames, one
+// 16-byte load each, with U runs per thread in flight: one CTA streams a
+// column of up to millions of frames, and one 4-byte load in flight per
+// thread left the kernel bound by memory latency.
+template <typename T>
+struct Run;
+template <>
+struct Run<float> {
+    using V = float4;
+    static constexpr int kN = 4;
+    static __device__ __forceinline__ float at(const float4 &v, int k) {
+        return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+    }
+};
+template <>
+struct Run<double> {
+    using V = double2;
+    static constexpr int kN = 2;
+    static __device__ __forceinline__ double at(const double2 &v, int k) { return k == 0 ? v.x : v.y; }
+};
+
+// run(f0, v) for every whole run this thread owns (f0 a multiple of kN when
+// the column starts on a 16-byte boundary), fn(f, x) for the single frames
+// before the first 16-byte boundary and after the last whole run.
+template <int U, int NT, typename T, typename Fn, typename RunFn>
+__device__ __forceinline__ void for_runs(const T *col, int F, int tid, Fn &&fn, RunFn &&run) {
+    using R = Run<T>;
+    using VT = typename R::V;
+    const int head = min(F, (int)(((16u - ((unsigned)(uintptr_t)col & 15u)) & 15u) / sizeof(T)));
+    if (tid < head) fn(tid, __ldg(col + tid));
+    const VT *cv = (const VT *)(col + head);
+    const int nv = (F - head) / R::kN;
+    int i = tid;
+    for (; i + (U - 1) * NT < nv; i += U * NT) {
+        VT x[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) x[u] = __ldg(cv + i + u * NT);
+#pragma unroll
+        for (int u = 0; u < U; u++) run(head + (i + u * NT) * R::kN, x[u]);
+    }
+    for (; i < nv; i += NT) run(head + i * R::kN, __ldg(cv + i));
+    const int t = head + nv * R::kN + tid;  // fewer than kN frames are left
+    if (t < F) fn(t, __ldg(col + t));
+}
+
+// fn(f, x) for every frame of the column, streamed as above
+template <int U, int NT, typename T, typename Fn>
+__device__ __forceinline__ void for_frames(const T *col, int F, int tid, Fn &&fn) {
+    for_runs<U, NT>(col, F, tid, fn, [&](int f0, const typename Run<T>::V &v) {
+#pragma unroll
+        for (int k = 0; k < Run<T>::kN; k++) fn(f0 + k, Run<T>::at(v, k));
+    });
+}
+constexpr int kUnroll = 2;
+constexpr int kMinBlocks = 2;  // CTAs per SM (64 registers a thread)
+constexpr int kTail = 256;  // bins per chunk of the per-DOF sums
 
 // One CTA's work on DOF g of one system; T is the input element type (float
 // or double). Every bin decision is screened in FP32 (see above) with an
@@ -126,15 +219,14 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
         // x / modfit_bs: relative error of x32 * fl32(1/bs) <= 2^-23 (2^-22.4
         // with the FP32 rounding of an FP64 input)
         const float rm = __double2float_rn(__drcp_rn(modfit_bs));
-        for (int f = tid; f < F; f += kThreads) {
-            const T xv = __ldg(colT + f);
+        for_frames<kUnroll, kThreads>(colT, F, tid, [&](int, T xv) {
             const float x = (float)xv;
             const float q = __fmul_rn(x, rm);
             int idx = screened_floor(q, __fmul_ru(q, kQRel));
             if (idx < 0) idx = __double2int_rz(__ddiv_rn((double)xv, modfit_bs));
             if (idx < 0 || idx >= kModfitBins) { bad++; idx = idx < 0 ? 0 : kModfitBins - 1; }
             atomicAdd(&hmod[warp * kModfitBins + idx], 1u);
-        }
+        });
         if (bad) atomicAdd(&err[ERR_MODFIT_RANGE], bad);
         __syncthreads();
         for (int k = tid; k < kModfitBins; k += kThreads) {
@@ -180,12 +272,12 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     const F2 mf2 = split2(modfit), tp2 = split2(twopi);
     const float r2pi = __double2float_rn(__drcp_rn(twopi));
     constexpr float kShiftEps = 4e-6f;
-    // exact quotient q of the shift of value xd (x = its FP32 rounding):
-    // screened, else FP64
-    auto shift_q = [&](float x, double xd, float &t32) -> int {
-        t32 = __fadd_rn(__fadd_rn(x, mf2.hi), mf2.lo);
+    // exact quotient q of the shift of value xv: screened on its FP32
+    // rounding, else FP64
+    auto shift_q = [&](T xv, float &t32) -> int {
+        t32 = __fadd_rn(__fadd_rn((float)xv, mf2.hi), mf2.lo);
         int q = screened_floor(__fmul_rn(t32, r2pi), kShiftEps);
-        if (q < 0) q = shift_quot(__dadd_rn(xd, modfit), twopi);
+        if (q < 0) q = shift_quot(__dadd_rn((double)xv, modfit), twopi);
         return q;
     };
 
@@ -195,19 +287,19 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     // then the shifted FP64 value of each candidate
     double lmax = -1.0e100, lmin = 1.0e100;
     {
-        unsigned long long kmax[kRegions], kmin[kRegions];
-        for (int r = 0; r < kRegions; r++) { kmax[r] = 0ull; kmin[r] = ~0ull; }
-        for (int f = tid; f < F; f += kThreads) {
-            const T xv = __ldg(colT + f);
-            const double xd = (double)xv;
+        using Key = OKey<T>;
+        using K = typename Key::K;
+        K kmax[kRegions], kmin[kRegions];
+        for (int r = 0; r < kRegions; r++) { kmax[r] = 0; kmin[r] = Key::kNone; }
+        for_frames<kUnroll, kThreads>(colT, F, tid, [&](int, T xv) {
             int r = 0;
             if (type == TD) {
                 float t32;
-                r = shift_q((float)xv, xd, t32);
+                r = shift_q(xv, t32);
                 r = r < 0 ? 0 : (r >= kRegions ? kRegions - 1 : r);  // out of range: flagged above
             }
-            const bool nan = is_nan_bits(xd);
-            const unsigned long long k = okey_raw(xd);
+            const bool nan = Key::nan(xv);
+            const K k = Key::key(xv);
 #pragma unroll
             for (int q = 0; q < kRegions; q++) {
                 if (q == r && !nan) {
@@ -215,12 +307,12 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
                     kmin[q] = k < kmin[q] ? k : kmin[q];
                 }
             }
-        }
+        });
         __shared__ unsigned long long red_kmax[kWarps][kRegions], red_kmin[kWarps][kRegions];
         for (int q = 0; q < kRegions; q++) {
             for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmax[q], o);
-                const unsigned long long b = __shfl_xor_sync(0xffffffffu, kmin[q], o);
+                const K a = __shfl_xor_sync(0xffffffffu, kmax[q], o);
+                const K b = __shfl_xor_sync(0xffffffffu, kmin[q], o);
                 kmax[q] = a > kmax[q] ? a : kmax[q];
                 kmin[q] = b < kmin[q] ? b : kmin[q];
             }
@@ -229,13 +321,13 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
         __syncthreads();
         if (tid == 0) {
             for (int q = 0; q < kRegions; q++) {
-                unsigned long long a = 0ull, b = ~0ull;
+                unsigned long long a = 0ull, b = Key::kNone;
                 for (int w = 0; w < kWarps; w++) {
                     a = red_kmax[w][q] > a ? red_kmax[w][q] : a;
                     b = red_kmin[w][q] < b ? red_kmin[w][q] : b;
                 }
                 if (a < b) continue;  // empty region
-                double va = okey_double(a), vb = okey_double(b);
+                double va = Key::value(a), vb = Key::value(b);
                 if (type == TD) {
                     va = shifted(va, modfit, twopi);
                     vb = shifted(vb, modfit, twopi);
@@ -288,15 +380,16 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
         double E = fabs(mn) + fabs(mx);
         if (type == TD) E = E + 2.0 * fabs(modfit) + 4.0 * twopi;
         const float e1 = __double2float_ru(E * 0x1p-20 / bs1), e2 = __double2float_ru(E * 0x1p-20 / bs2);
-        for (int f = tid; f < F; f += kThreads) {
-            const T xin = __ldg(colT + f);
+        // both bin indices of one value, counted in the 1D histograms; the 2D
+        // bin is returned for the pair kernels' bin matrices
+        auto bin_of = [&](T xin) -> int {
             const float x = (float)xin;
             float d32;
             int q = 0;
             if (type == TD) {
                 float t32;
-                q = shift_q(x, (double)xin, t32);
-                const float qf = (float)q;
+                q = shift_q(xin, t32);
+                const float qf = q >= 0 ? small_int_float(q) : (float)q;
                 d32 = __fsub_rn(__fsub_rn(__fsub_rn(__fsub_rn(t32, __fmul_rn(qf, tp2.hi)), __fmul_rn(qf, tp2.lo)),
                                           mn2.hi),
                                 mn2.lo);
@@ -316,9 +409,23 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
             if (i2 < 0 || i2 >= B2) { bad++; i2 = i2 < 0 ? 0 : B2 - 1; }
             atomicAdd(&h1[w1 * B1 + i1], 1u);
             atomicAdd(&h2[warp * B2 + i2], 1u);
-            // every bin matrix of the layout the pair kernel reads
-            store_bin(bins, geo, g, f, i2);
-        }
+            return i2;
+        };
+        // every bin matrix of the layout the pair kernels read: a whole run
+        // in one store per matrix where it starts on a multiple of its length
+        for_runs<kUnroll, kThreads>(
+            colT, F, tid, [&](int f, T xin) { store_bin(bins, geo, g, f, bin_of(xin)); },
+            [&](int f0, const typename Run<T>::V &v) {
+                int b[Run<T>::kN];
+#pragma unroll
+                for (int k = 0; k < Run<T>::kN; k++) b[k] = bin_of(Run<T>::at(v, k));
+                if ((f0 & (Run<T>::kN - 1)) == 0) {
+                    store_bin_run<Run<T>::kN>(bins, geo, g, f0, b);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < Run<T>::kN; k++) store_bin(bins, geo, g, f0 + k, b[k]);
+                }
+            });
     }
     if (bad) atomicAdd(&err[ERR_BIN_RANGE], bad);
     __syncthreads();
@@ -332,67 +439,100 @@ __device__ __forceinline__ void prep_body(const SysGeom &geo, const void *cb, co
     }
     __syncthreads();
 
-    if (tid == 0) {
-        // largest 2D-bin marginal count: no 2D bin of a pair with this DOF
-        // can hold more frames
-        unsigned int m2 = 0;
-        for (int k = 0; k < B2; k++) m2 = h2[k] > m2 ? h2[k] : m2;
-        dof.m2[g] = (int)m2;
+    // ---- per-DOF sums on warp 0: lane 0 runs the reference's sequential
+    // recurrences and sums, the 32 lanes take the per-bin logarithms and
+    // sines (each FP64 warp instruction costs the same with 1 or 32 lanes
+    // active, and the FP64 pipe is a small fraction of this part's rate)
+    if (warp == 0) {
+        __shared__ double s_x[kTail], s_t[kTail];
+        __shared__ unsigned char s_f[kTail];
+        const int N = F;
+        // lane 0: x_k = x_{k-1} + step for the bins [c0, c0 + n) (the
+        // reference's repeated +=, carried across chunks in x)
+        auto points = [&](double &x, double step, int n) {
+            if (lane == 0)
+                for (int k = 0; k < n; k++) {
+                    s_x[k] = x;
+                    x = __dadd_rn(x, step);
+                }
+            __syncwarp();
+        };
+        // lane 0: sum of the flagged terms in bin order, counting them
+        auto sum_terms = [&](double &sum, int &count, int n) {
+            __syncwarp();
+            if (lane == 0)
+                for (int k = 0; k < n; k++)
+                    if (s_f[k]) {
+                        sum = sum + s_t[k];
+                        count++;
+                    }
+            __syncwarp();
+        };
 
         // 1D entropy in the reference's order (PARENT.cpp:658-670, 702-714, 746-756)
-        const int N = F;
         int occupbins = 0;
-        double plnpsum = 0.0, probDens;
-        if (type == TB) {
-            double blen = __dadd_rn(mn, bs1 / 2.0);
-            for (int k = 0; k < B1; k++) {
-                probDens = (double)h1[k] / (((N * bs1) * blen) * blen);
-                if (probDens > 0) {
-                    plnpsum = plnpsum + ((blen * blen) * probDens) * log(probDens);
-                    occupbins++;
+        double plnpsum = 0.0, x1 = __dadd_rn(mn, bs1 / 2.0);
+        for (int c0 = 0; c0 < B1; c0 += kTail) {
+            const int n = min(kTail, B1 - c0);
+            if (type != TD) points(x1, bs1, n);
+            for (int k = lane; k < n; k += 32) {
+                const double h = (double)h1[c0 + k];
+                double probDens, t = 0.0;
+                if (type == TB) {
+                    const double blen = s_x[k];
+                    probDens = h / (((N * bs1) * blen) * blen);
+                    if (probDens > 0) t = ((blen * blen) * probDens) * log(probDens);
+                } else if (type == TA) {
+                    const double st = sin(s_x[k]);
+                    probDens = h / ((N * bs1) * st);
+                    if (probDens > 0) t = (st * probDens) * log(probDens);
+                } else {
+                    probDens = h / (N * bs1);
+                    if (probDens > 0) t = probDens * log(probDens);
                 }
-                blen = __dadd_rn(blen, bs1);
+                s_t[k] = t;
+                s_f[k] = probDens > 0;
             }
-        } else if (type == TA) {
-            double theta = __dadd_rn(mn, bs1 / 2.0);
-            for (int k = 0; k < B1; k++) {
-                const double st = sin(theta);
-                probDens = (double)h1[k] / ((N * bs1) * st);
-                if (probDens > 0) {
-                    plnpsum = plnpsum + (st * probDens) * log(probDens);
-                    occupbins++;
-                }
-                theta = __dadd_rn(theta, bs1);
-            }
-        } else {
-            for (int k = 0; k < B1; k++) {
-                probDens = (double)h1[k] / (N * bs1);
-                if (probDens > 0) {
-                    plnpsum = plnpsum + probDens * log(probDens);
-                    occupbins++;
-                }
-            }
+            sum_terms(plnpsum, occupbins, n);
         }
-        plnpsum = -plnpsum * bs1;
-        dof.s1[g] = plnpsum + (occupbins - 1.0) / (2.0 * N);
 
         // A = ln(bs2) + (1/N) sum_k m(k) ln J(c_k), with c_k advanced by
         // repeated += binsize as the reference's 2D epilogues do
         // (e.g. PARENT.cpp:807-820); J = c^2 (bond), sin c (angle), 1 (dihedral).
-        double acc = 0.0;
-        if (type != TD) {
-            double c = __dadd_rn(mn, bs2 / 2.0);
-            for (int k = 0; k < B2; k++) {
-                if (h2[k]) acc += (double)h2[k] * (type == TB ? log(c * c) : log(sin(c)));
-                c = __dadd_rn(c, bs2);
+        double acc = 0.0, x2 = __dadd_rn(mn, bs2 / 2.0);
+        int unused = 0;
+        unsigned int m2 = 0;
+        for (int c0 = 0; c0 < B2; c0 += kTail) {
+            const int n = min(kTail, B2 - c0);
+            if (type != TD) points(x2, bs2, n);
+            for (int k = lane; k < n; k += 32) {
+                const unsigned int h = h2[c0 + k];
+                m2 = h > m2 ? h : m2;
+                if (type != TD && h) {
+                    const double c = s_x[k];
+                    s_t[k] = (double)h * (type == TB ? log(c * c) : log(sin(c)));
+                }
+                s_f[k] = type != TD && h != 0u;
             }
+            sum_terms(acc, unused, n);
         }
-        dof.acon[g] = log(bs2) + acc / (double)N;
+        // largest 2D-bin marginal count: no 2D bin of a pair with this DOF
+        // can hold more frames
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned int v = __shfl_xor_sync(0xffffffffu, m2, o);
+            m2 = v > m2 ? v : m2;
+        }
+        if (lane == 0) {
+            dof.m2[g] = (int)m2;
+            plnpsum = -plnpsum * bs1;
+            dof.s1[g] = plnpsum + (occupbins - 1.0) / (2.0 * N);
+            dof.acon[g] = log(bs2) + acc / (double)N;
+        }
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void *cb, const void *ca, const void *cd,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) prep_kernel(SysGeom geo, const void *cb, const void *ca, const void *cd,
                                                         int64_t ld, int prec, DofArrays dof, uint8_t *bins, int *err,
                                                         double modfit_bs, double pi, int g_first, int h1_copies) {
     prep_body<T>(geo, cb, ca, cd, ld, prec, dof, bins, err, modfit_bs, pi, g_first + blockIdx.x, h1_copies);
@@ -401,7 +541,7 @@ __global__ void __launch_bounds__(kThreads) prep_kernel(SysGeom geo, const void 
 // Many systems in one launch: CTA k preprocesses DOF map[k].y of system
 // map[k].x (systems of one input precision per launch).
 template <typename T>
-__global__ void __launch_bounds__(kThreads) prep_batch_kernel(const PrepDesc *__restrict__ sys,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) prep_batch_kernel(const PrepDesc *__restrict__ sys,
                                                               const int2 *__restrict__ map, int *err,
                                                               double modfit_bs, double pi, int h1_copies) {
     const int2 m = map[blockIdx.x];
