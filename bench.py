@@ -246,6 +246,53 @@ def parity_on_sample(eng, bins, form):
             "counts": "bit-exact (tests/test_gpu_parity.py)"}
 
 
+def reference_exe():
+    """The reference's own PARENT.x compiled from its sources (oracle/Makefile
+    ref), if it was built and runs on this machine's architecture."""
+    exe = ROOT / "oracle" / "_ref" / "PARENT.x"
+    if not os.access(exe, os.X_OK):
+        return None
+    try:
+        subprocess.run([str(exe)], capture_output=True, timeout=60)  # usage text, exit 1
+    except OSError:  # built for another architecture
+        return None
+    return exe
+
+
+def cpu_sample_reference(args, wl, exe):
+    """The reference's own PARENT.x on the CPU sample of cpu_sample (written as
+    a .bat file), all host threads: updates/s of its own "Calculation time"
+    (the read of the .bat and the .par write excluded)."""
+    import re
+    import shutil
+    import parent_gb300 as pg
+    n_atoms, F, prec, fbd, fbb, lat = wl
+    threads = os.cpu_count() or 1
+    na = args.cpu_sample_atoms
+    if na <= 0:
+        dofs = int((2 * 8e10 / F) ** 0.5)
+        na = max(6, min(n_atoms, dofs // 3 + 2))
+    t = pg.synth_host(na, F, double_prec=prec, seed=1234, n_latents=lat, frac_bimodal_dih=fbd,
+                      frac_bimodal_bond=fbb)
+    D = 3 * na - 6
+    units = D * (D - 1) // 2 * F
+    d = Path(tempfile.mkdtemp(prefix="pg_ref_"))
+    try:
+        pg.write_bat(d / "s.bat", t)
+        del t
+        r = subprocess.run([str(exe), str(d / "s.bat"), str(d / "s.par")] + [str(args.bins)] * 6,
+                           capture_output=True, text=True, env={**os.environ, "OMP_NUM_THREADS": str(threads)})
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    m = re.search(r"Calculation time: ([0-9.eE+-]+)", r.stdout)
+    if r.returncode != 0 or m is None:
+        raise RuntimeError("PARENT.x failed: " + (r.stdout + r.stderr)[-500:])
+    dt = float(m.group(1))
+    sample = (f"{D} DOFs ({na} atoms) x {F} frames of the same generator as a .bat, {units:.3e} updates, "
+              f"{dt:.2f} s of the reference's own calculation time (MPI: one rank)")
+    return units / dt, sample, threads, dt
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     # the batch workload is sampled as one system of its largest atom count at
@@ -253,9 +300,16 @@ def run_reference(args):
     wl = WORKLOADS[args.workload] if args.workload in WORKLOADS else (800, 31_700, 0, 0.0, 0.0, 8)
     if rank != 0:
         return 0
+    # the reference's own binary where it was built here (this architecture),
+    # else the oracle port of its algorithm
+    exe = reference_exe()
+    kind = "reference" if exe is not None else "port"
     vals = []
     for i in range(args.warmup + args.steps):
-        v, sample, threads, dt = cpu_sample(args, wl)
+        if exe is not None:
+            v, sample, threads, dt = cpu_sample_reference(args, wl, exe)
+        else:
+            v, sample, threads, dt = cpu_sample(args, wl)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
@@ -266,7 +320,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "n_atoms": n_atoms, "frames": F, "bins": args.bins},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
