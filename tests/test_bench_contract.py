@@ -1,7 +1,8 @@
-"""bench.py's reference arm, run on CPU: `--impl reference` times the oracle
-port of the reference algorithm on a bounded DOF sample and prints one JSON
-line with the contract's keys; under a multi-rank launch only rank 0 runs and
-prints, the other ranks exit 0 without work."""
+"""bench.py's reference arm, run on CPU: `--impl reference` times the
+reference's own PARENT.x where it was built on this machine (oracle/_ref),
+else the oracle port of its algorithm, on a bounded DOF sample and prints one
+JSON line with the contract's keys; under a multi-rank launch only rank 0
+runs and prints, the other ranks exit 0 without work."""
 from __future__ import annotations
 
 import json
@@ -35,7 +36,10 @@ def test_reference_arm_prints_the_contract_line():
     assert d["value"] > 0 and d["higher_is_better"] is True and d["vs_baseline"] is None
     assert d["config"]["workload"] == "plain_294dof_20k"
     cb = d["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert cb["kind"] == ("reference" if bench.reference_exe() is not None else "port")
+    assert cb["cores"] >= 1 and cb["value"] == d["value"]
     assert "24 DOFs (10 atoms) x 20000 frames" in cb["sample"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
