@@ -167,18 +167,7 @@ static int fail(pg_ctx *c, int code, const char *fmt, ...) {
         }                                                                                            \
     } while (0)
 
-static DofArrays dof_arrays(pg_ctx *ctx, int D) {
-    DofArrays d;
-    double *base = (double *)ctx->dofbuf.p;
-    d.mn = base;
-    d.mx = base + D;
-    d.shift = base + 2 * (size_t)D;
-    d.s1 = base + 3 * (size_t)D;
-    d.acon = base + 4 * (size_t)D;
-    d.b2 = (int *)(base + 5 * (size_t)D);
-    d.m2 = d.b2 + D;
-    return d;
-}
+static DofArrays dof_arrays(pg_ctx *ctx, int D) { return dof_at(ctx->dofbuf.p, D); }
 
 static size_t elem_size(int prec) { return prec ? 8 : 4; }
 
@@ -261,7 +250,7 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int f
     CK(cudaEventRecord(ctx->ev[1], st));
 
     CK(ctx->bins.ensure(bins_bytes(g)));
-    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
+    CK(ctx->dofbuf.ensure(dof_bytes(D)));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
     CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
     if (ctx->nlogn_max < g.F) {
@@ -439,7 +428,7 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
     const ParLayout L = par_layout(g.n_dih);
     CK(ctx->cols.ensure((size_t)D * F * es + 256));
     CK(ctx->bins.ensure(bins_bytes(g)));
-    CK(ctx->dofbuf.ensure((size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64));
+    CK(ctx->dofbuf.ensure(dof_bytes(D)));
     CK(ctx->errw.ensure(ERR_WORDS * sizeof(int)));
     CK(ctx->par.ensure((size_t)L.total * sizeof(double)));
     CK(ctx->mi.ensure((size_t)D * D * sizeof(double)));
@@ -480,7 +469,8 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
     }
     const size_t sb32 = h32 ? pairs_hist32_scratch_bytes(bmax_of(g), pairs_hist32_grid((int64_t)ctx->tiles_host.size()))
                             : 0;
-    if (h32) CK(ctx->scratch.ensure(sb32));
+    // one scratch area (tile counter, overflow counts) per pair stream
+    if (h32) CK(ctx->scratch.ensure(2 * sb32));
 
     CK(cudaEventRecord(ctx->ev[0], st));
     CK(cudaStreamWaitEvent(cs, ctx->ev[0], 0));  // earlier kernels reading the columns are done
@@ -527,8 +517,6 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
         }
         for (auto &e : ctx->pev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    // the 16-bit layout's launches share one overflow area: keep them in order
-    const bool alternate = !(h32 && !pairs_hist32_wide(bmax_of(g)));
     for (int k = 0; k < K; k++) {
         CK(cudaStreamWaitEvent(st, ctx->gev[k], 0));
         CK(launch_prep(g, colp, F, tv->double_prec, dof, (uint8_t *)ctx->bins.p, (int *)ctx->errw.p, st, G[k],
@@ -538,12 +526,12 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
         CK(cudaEventRecord(ctx->pev[k], st));
         const int64_t n = cut[k + 1] - cut[k];
         if (n <= 0) continue;
-        cudaStream_t ps = ctx->pst[alternate ? (k & 1) : 0];
+        cudaStream_t ps = ctx->pst[k & 1];
         CK(cudaStreamWaitEvent(ps, ctx->pev[k], 0));
         if (h32)
             CK(launch_pairs_hist32(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
-                                   ctx->nfix_scale, tiles + cut[k], n, po, (int *)ctx->errw.p, ctx->scratch.p, sb32,
-                                   ps));
+                                   ctx->nfix_scale, tiles + cut[k], n, po, (int *)ctx->errw.p,
+                                   (char *)ctx->scratch.p + (k & 1) * sb32, sb32, ps));
         else
             CK(launch_pairs_hist(g, (const uint8_t *)ctx->bins.p, dof, (const unsigned long long *)ctx->nfix.p,
                                  ctx->nfix_scale, tiles + cut[k], n, T, po, (int *)ctx->errw.p, ps));
@@ -1437,7 +1425,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
         L.bins = off;
         off = al256(off + bins_bytes(g));
         L.dof = off;
-        off = al256(off + (size_t)g.D * (5 * sizeof(double) + 2 * sizeof(int)) + 64);
+        off = al256(off + dof_bytes(g.D));
         L.par = off;
         off = al256(off + (size_t)par_layout(g.n_dih).total * sizeof(double));
         L.mi = off;
@@ -1463,19 +1451,7 @@ PG_API int pg_entropy_batch(pg_ctx *ctx, int n_sys, const pg_bat_view *trajs, co
     if (!pairs_hist_config(bmax, &T, &fc, &nst)) return fail(ctx, PG_ERR_UNSUPPORTED, "2D bins too large");
 
     // ---- descriptors and the concatenated tile list
-    auto dofs_at = [&](const BatchLayout &L) {
-        DofArrays d;
-        double *b = (double *)(arena + L.dof);
-        const int D = L.g.D;
-        d.mn = b;
-        d.mx = b + D;
-        d.shift = b + 2 * (size_t)D;
-        d.s1 = b + 3 * (size_t)D;
-        d.acon = b + 4 * (size_t)D;
-        d.b2 = (int *)(b + 5 * (size_t)D);
-        d.m2 = d.b2 + D;
-        return d;
-    };
+    auto dofs_at = [&](const BatchLayout &L) { return dof_at(arena + L.dof, L.g.D); };
     std::vector<SysDesc> sd((size_t)n_sys);
     std::vector<MistDesc> md((size_t)n_sys);
     std::vector<PairTile> tiles;

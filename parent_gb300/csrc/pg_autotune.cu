@@ -111,21 +111,11 @@ cudaError_t make_probe(Probe &p, const SysGeom &like, int D, int F, cudaStream_t
     }
     if ((e = cudaMemcpyAsync(p.bins, h.data(), nbins, cudaMemcpyHostToDevice, st))) return e;
     double *dd = nullptr;
-    if ((e = p.alloc((void **)&dd, (size_t)g.D * (5 * sizeof(double) + 2 * sizeof(int))))) return e;
-    std::vector<double> hd((size_t)g.D * 5, 0.0);
-    std::vector<int> hi((size_t)g.D * 2, 0);
-    for (int d = 0; d < g.D; d++) {
-        hi[d] = g.bins[3 + dof_type(d, g.nb, g.na)];  // b2
-        hi[g.D + d] = 0;                               // m2: no 16-bit folds
-    }
-    p.dof.mn = dd;
-    p.dof.mx = dd + g.D;
-    p.dof.shift = dd + 2 * (size_t)g.D;
-    p.dof.s1 = dd + 3 * (size_t)g.D;
-    p.dof.acon = dd + 4 * (size_t)g.D;
-    p.dof.b2 = (int *)(dd + 5 * (size_t)g.D);
-    p.dof.m2 = p.dof.b2 + g.D;
-    if ((e = cudaMemcpyAsync(dd, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice, st))) return e;
+    if ((e = p.alloc((void **)&dd, dof_bytes(g.D)))) return e;
+    if ((e = cudaMemsetAsync(dd, 0, dof_bytes(g.D), st))) return e;  // m2 0: no 16-bit folds
+    std::vector<int> hi((size_t)g.D, 0);
+    for (int d = 0; d < g.D; d++) hi[d] = g.bins[3 + dof_type(d, g.nb, g.na)];  // b2
+    p.dof = dof_at(dd, g.D);
     if ((e = cudaMemcpyAsync(p.dof.b2, hi.data(), hi.size() * sizeof(int), cudaMemcpyHostToDevice, st))) return e;
     const ParLayout L = par_layout(g.n_dih);
     if ((e = p.alloc((void **)&p.out.par, (size_t)L.total * sizeof(double)))) return e;

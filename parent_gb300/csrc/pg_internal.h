@@ -105,6 +105,21 @@ struct DofArrays {
     int *m2;                 // largest marginal count over the DOF's 2D bins
 };
 
+// One system's DofArrays in one allocation of dof_bytes(D) bytes at base
+inline size_t dof_bytes(int D) { return (size_t)D * (5 * sizeof(double) + 2 * sizeof(int)) + 64; }
+inline DofArrays dof_at(void *base, int D) {
+    DofArrays d;
+    double *b = (double *)base;
+    d.mn = b;
+    d.mx = b + D;
+    d.shift = b + 2 * (size_t)D;
+    d.s1 = b + 3 * (size_t)D;
+    d.acon = b + 4 * (size_t)D;
+    d.b2 = (int *)(b + 5 * (size_t)D);
+    d.m2 = d.b2 + D;
+    return d;
+}
+
 // Offsets of the nine .par body blocks inside one contiguous double buffer.
 struct ParLayout {
     int64_t s1b, s1a, s1d, bb, ba, bd, aa, ad, dd, total;
