@@ -79,8 +79,10 @@ typedef struct pg_bat_view {
  * io_binary.cpp:606-631): same-type blocks bb/aa/dd store pair #(P-1-k) at
  * element k, i.e. reverse lexicographic order (PARENT.cpp:1107-1112);
  * ba/bd/ad are row-major with the bond (resp. angle) index slow.
- * Host pointers owned by the caller; sizes nB, nA, nD, nB(nB-1)/2, nB*nA,
- * nB*nD, nA(nA-1)/2, nA*nD, nD(nD-1)/2 doubles. */
+ * Pointers owned by the caller, to host memory or to device memory of the
+ * context's GPU (the copies take their direction from the pointers); sizes
+ * nB, nA, nD, nB(nB-1)/2, nB*nA, nB*nD, nA(nA-1)/2, nA*nD, nD(nD-1)/2
+ * doubles. */
 typedef struct pg_par_body {
     double *s1_b, *s1_a, *s1_d;
     double *bb, *ba, *bd, *aa, *ad, *dd;

@@ -190,6 +190,26 @@ class ParBody:
         return np.concatenate([self.blocks[k] for k in block_sizes(self.n_dih)])
 
 
+class DeviceParBody:
+    """A .par body in device memory of the engine's GPU: one flat buffer of
+    doubles in block_sizes order (e.g. a torch CUDA tensor's data_ptr()),
+    usable as the output of Engine.entropy_shard and the input of
+    Engine.mist, so a sharded body can be reduced and fed to MIST without
+    passing through the host."""
+
+    def __init__(self, n_dih: int, ptr: int):
+        self.n_dih = n_dih
+        self.ptr = int(ptr)
+
+    def c(self) -> ParBodyC:
+        b = ParBodyC()
+        o = 0
+        for k, n in block_sizes(self.n_dih).items():
+            setattr(b, k, C.cast(C.c_void_p(self.ptr + 8 * o), C.POINTER(C.c_double)))
+            o += n
+        return b
+
+
 @dataclass
 class Trajectory:
     """DOF-major columns: bonds (nDih+2, F), angles (nDih+1, F), dihedrals (nDih, F)."""
@@ -303,8 +323,9 @@ class Engine:
         _check(lib().pg_write_mie_text_device(self._ctx, str(path).encode() if path else None, body.n_dih,
                                               C.byref(bc)), self._ctx)
 
-    def mist(self, n_dih: int, body: ParBody | None = None):
-        """MIST tree: (edges as a structured numpy array, totals[10])."""
+    def mist(self, n_dih: int, body: "ParBody | DeviceParBody | None" = None):
+        """MIST tree: (edges as a structured numpy array, totals[10]), from the
+        resident MI matrix or from a host or device body."""
         n = 3 * n_dih + 2
         edges = (MistEdge * max(n, 1))()
         totals = (C.c_double * 10)()
@@ -343,13 +364,15 @@ class Engine:
         return outs, res
 
     def entropy_shard(self, traj: Trajectory | BatView, bins, shard: int, n_shards: int,
-                      form: str | int = "auto") -> ParBody:
+                      form: str | int = "auto", out: "ParBody | DeviceParBody | None" = None):
         """Shard `shard` of `n_shards` of PARENT.x (pg_entropy_shard): this shard's
-        2D entropies (and, for shard 0, the 1D entropies), zeros elsewhere."""
+        2D entropies (and, for shard 0, the 1D entropies), zeros elsewhere,
+        into `out` (host or device body; a new host body by default)."""
         v = traj if isinstance(traj, BatView) else traj.view()
         b = (C.c_int * 6)(*bins)
         f = FORMS[form] if isinstance(form, str) else int(form)
-        out = ParBody.empty(v.n_dihedrals)
+        if out is None:
+            out = ParBody.empty(v.n_dihedrals)
         body = out.c()
         _check(lib().pg_entropy_shard(self._ctx, C.byref(v), b, f, shard, n_shards, C.byref(body)), self._ctx)
         return out

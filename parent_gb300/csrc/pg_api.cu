@@ -268,7 +268,9 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int f
 }
 
 // Enqueues the copies of a device .par body (layout L) into the caller's
-// host blocks; every non-empty block needs a destination.
+// blocks (host memory, or device memory of this context's GPU: the copy
+// direction comes from the pointers); every non-empty block needs a
+// destination.
 static int body_to_host(pg_ctx *ctx, const double *par, const ParLayout &L, const pg_par_body *out, int sys) {
     double *dst[9] = {out->s1_b, out->s1_a, out->s1_d, out->bb, out->ba, out->bd, out->aa, out->ad, out->dd};
     const int64_t off[10] = {L.s1b, L.s1a, L.s1d, L.bb, L.ba, L.bd, L.aa, L.ad, L.dd, L.total};
@@ -279,7 +281,7 @@ static int body_to_host(pg_ctx *ctx, const double *par, const ParLayout &L, cons
             if (sys >= 0) return fail(ctx, PG_ERR_ARG, "system %d: null output block %d", sys, k);
             return fail(ctx, PG_ERR_ARG, "null output block %d", k);
         }
-        CK(cudaMemcpyAsync(dst[k], par + off[k], (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(dst[k], par + off[k], (size_t)n * sizeof(double), cudaMemcpyDefault, ctx->stream));
     }
     return PG_OK;
 }
@@ -1128,12 +1130,10 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
             const int64_t n = off[k + 1] - off[k];
             if (n <= 0) continue;
             if (!src[k]) return fail(ctx, PG_ERR_ARG, "null body block %d", k);
-            CK(cudaMemcpyAsync((double *)ctx->par.p + off[k], src[k], (size_t)n * sizeof(double),
-                               cudaMemcpyHostToDevice, st));
+            // host or device blocks: the copy direction comes from the pointers
+            CK(cudaMemcpyAsync((double *)ctx->par.p + off[k], src[k], (size_t)n * sizeof(double), cudaMemcpyDefault,
+                               st));
         }
-        memcpy(s1.data(), body->s1_b, nb * sizeof(double));
-        memcpy(s1.data() + nb, body->s1_a, na * sizeof(double));
-        if (nd) memcpy(s1.data() + nb + na, body->s1_d, nd * sizeof(double));
         CK(launch_mi_from_par(n_dihedrals, (const double *)ctx->par.p, L, (double *)ctx->mi.p, st));
         ctx->launches++;
         ctx->resident = false;
@@ -1149,8 +1149,9 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     CK(launch_mist_impl(D, nb, na, (const double *)ctx->mi.p, ctx->mistscr.p, emi, efrom, eto, st));
     ctx->launches++;
     CK(cudaEventRecord(ctx->ev[2], st));
-    if (!body)
-        CK(cudaMemcpyAsync(h_s1, dof_arrays(ctx, D).s1, (size_t)D * sizeof(double), cudaMemcpyDeviceToHost, st));
+    // the 1D entropies (s1_b | s1_a | s1_d lead the body layout)
+    CK(cudaMemcpyAsync(h_s1, body ? (const double *)ctx->par.p + L.s1b : dof_arrays(ctx, D).s1,
+                       (size_t)D * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (D > 1) {
         CK(cudaMemcpyAsync(hmi, emi, (size_t)(D - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(hf, efrom, (size_t)(D - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1158,7 +1159,7 @@ PG_API int pg_mist(pg_ctx *ctx, int n_dihedrals, const pg_par_body *body, pg_mis
     }
     CK(cudaEventRecord(ctx->ev[3], st));
     CK(cudaStreamSynchronize(st));
-    if (!body) memcpy(s1.data(), h_s1, (size_t)D * sizeof(double));
+    memcpy(s1.data(), h_s1, (size_t)D * sizeof(double));
     float ms[3];
     cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[1]);
     cudaEventElapsedTime(&ms[1], ctx->ev[1], ctx->ev[2]);

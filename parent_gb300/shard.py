@@ -13,7 +13,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import ParBody, _check, block_sizes, lib
+from . import DeviceParBody, ParBody, _check, block_sizes, lib
 
 
 def shard_mask(n_dih: int, bins, shard: int, n_shards: int) -> np.ndarray:
@@ -45,9 +45,32 @@ def merge_bodies(n_dih: int, local: np.ndarray, dist=None, device: str = "cpu") 
     return body_from_flat(n_dih, t.cpu().numpy())
 
 
-def entropy_sharded(eng, traj, bins, dist=None, device: str = "cpu", form: str = "auto") -> ParBody | None:
-    """PARENT.x over all ranks of `dist` (or alone): rank 0 returns the body."""
+def entropy_sharded(eng, traj, bins, dist=None, device: str = "cpu", form: str = "auto",
+                    on_device: bool = False):
+    """PARENT.x over all ranks of `dist` (or alone): rank 0 returns the body.
+
+    With a CUDA `device` (the engine's GPU) each rank's shard is written
+    straight into a device tensor, the SUM reduction runs on it (NCCL), and
+    rank 0 gets the host body, or with on_device=True a DeviceParBody (its
+    tensor attached as `.tensor`) that Engine.mist reads without a host copy.
+    Otherwise the shards are host arrays reduced on `device` (gloo on CPU)."""
     rank, world = (dist.get_rank(), dist.get_world_size()) if dist is not None else (0, 1)
     n_dih = traj.n_dihedrals if hasattr(traj, "n_dihedrals") else traj.n_dih
+    if str(device).startswith("cuda"):
+        import torch
+        total = sum(block_sizes(n_dih).values())
+        t = torch.zeros(total, dtype=torch.float64, device=device)
+        torch.cuda.synchronize(t.device)  # the zeros are written before the engine's stream writes
+        eng.entropy_shard(traj, bins, rank, world, form, out=DeviceParBody(n_dih, t.data_ptr()))
+        if dist is not None:
+            dist.reduce(t, dst=0, op=dist.ReduceOp.SUM)
+        if rank != 0:
+            return None
+        if on_device:
+            torch.cuda.synchronize(t.device)
+            body = DeviceParBody(n_dih, t.data_ptr())
+            body.tensor = t
+            return body
+        return body_from_flat(n_dih, t.cpu().numpy())
     part = eng.entropy_shard(traj, bins, rank, world, form)
     return merge_bodies(n_dih, part.flat(), dist, device)

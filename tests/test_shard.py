@@ -118,6 +118,37 @@ def test_gpu_shards_sum_to_the_whole(monkeypatch, n_atoms, F, bins, n_shards, st
 
 
 @pytest.mark.gpu
+def test_gpu_shards_into_device_memory():
+    """Shard bodies written straight into CUDA tensors (DeviceParBody), summed
+    on the device, equal the pg_entropy body bit for bit; entropy_sharded with
+    a CUDA device keeps the merged body there, and MIST read from it gives the
+    tree of the host body."""
+    torch = pytest.importorskip("torch")
+    t = pg.synth_host(50, 12000, double_prec=0, seed=8, frac_bimodal_dih=0.2)
+    n, bins, k = 47, (50,) * 6, 3
+    with pg.Engine(0) as eng:
+        whole = eng.entropy(t, bins, "hist")
+        total = whole.flat().size
+        acc = torch.zeros(total, dtype=torch.float64, device="cuda:0")
+        for s in range(k):
+            part = torch.full((total,), float("nan"), dtype=torch.float64, device="cuda:0")
+            torch.cuda.synchronize()
+            eng.entropy_shard(t, bins, s, k, out=pg.DeviceParBody(n, part.data_ptr()))
+            mask = torch.from_numpy(sh.shard_mask(n, bins, s, k)).to("cuda:0")
+            assert not torch.any(part[~mask] != 0)  # every entry written, zeros outside the shard
+            acc += part
+        assert np.array_equal(acc.cpu().numpy().view(np.uint64), whole.flat().view(np.uint64))
+        dev = sh.entropy_sharded(eng, t, bins, device="cuda:0", on_device=True)
+        assert isinstance(dev, pg.DeviceParBody)
+        assert np.array_equal(dev.tensor.cpu().numpy().view(np.uint64), whole.flat().view(np.uint64))
+        e1, t1 = eng.mist(n, dev)
+        e2, t2 = eng.mist(n, whole)
+        assert np.array_equal(e1, e2) and np.array_equal(t1, t2)
+        host = sh.entropy_sharded(eng, t, bins, device="cuda:0")
+        assert np.array_equal(host.flat().view(np.uint64), whole.flat().view(np.uint64))
+
+
+@pytest.mark.gpu
 def test_gpu_shard_rejects_onehot_and_bad_index():
     t = pg.synth_host(10, 2000, double_prec=0, seed=1)
     with pg.Engine(0) as eng:
