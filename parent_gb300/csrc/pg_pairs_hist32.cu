@@ -437,6 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32_kernel(const __grid_
 // warps meet only at the end of a tile (and at the 16-bit folds). Counting,
 // folds and the epilogue are those of the ring kernel.
 constexpr int kFoldGroups = kFoldFrames / 16;
+constexpr int kQueue = 32;  // finished tiles per FP64 epilogue round (one per warp)
 
 // 16 bytes from global memory, not kept in L1 (each line is read once)
 __device__ __forceinline__ uint4 ldg_stream(const void *p) {
@@ -504,6 +505,13 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid
     __shared__ unsigned long long s_snl[32];
     __shared__ unsigned int s_occ[32];
     __shared__ int s_heavy[32];
+    // sums of finished tiles whose FP64 epilogue waits for kQueue of them;
+    // then warp q finishes the pairs of tile q (the FP64 pipe is a small
+    // fraction of this part's rate, and one warp finishing every tile
+    // alone held back the next tile, whose frame groups are split evenly
+    // over all warps)
+    __shared__ unsigned long long s_qsnl[kQueue][32];
+    __shared__ unsigned int s_qocc[kQueue][32];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid * 4; i < nwords; i += kThreads * 4) *(uint4 *)(hist + i) = make_uint4(0u, 0u, 0u, 0u);
@@ -518,7 +526,9 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid
     const int pr = lane / kCols, pc = lane % kCols;
     const uint32_t hbase = smem_u32(hist) + lane * 4;
     uint32_t *ovf = a.ovf_all + (size_t)blockIdx.x * 2 * nwords;  // [bin][lane]
-    for (int64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+    for (int it = 0;; it++) {
+        const int64_t t = blockIdx.x + (int64_t)it * gridDim.x;
+        if (t >= a.n_tiles) break;
         const SysDesc &d = sys_of(t);
         const PairTile tile = a.tiles[t];
         const int F = d.geo.F, D = d.geo.D;
@@ -667,23 +677,63 @@ __global__ void __launch_bounds__(kThreads, 1) pairs_hist32s_kernel(const __grid
             atomicAdd(&s_occ[lane], (unsigned int)occ);
         }
         __syncthreads();
-        if (tid < 32) {
-            if (valid) {
-                const double N = (double)F;
-                const double sn = (double)s_snl[tid] / a.fix;
-                const int o = (int)s_occ[tid];
-                const double S2 = d.lnN + d.dof.acon[gr] + d.dof.acon[gc] - sn / N + (o - 1.0) / (2.0 * N);
-                if (d.out.par) d.out.par[par_pair_index(d.out.L, d.geo.nb, d.geo.na, d.geo.nd, gr, gc)] = S2;
-                if (d.out.mi) {
-                    const double mi = d.dof.s1[gr] + d.dof.s1[gc] - S2;
-                    d.out.mi[(int64_t)gr * d.geo.D + gc] = mi;
-                    d.out.mi[(int64_t)gc * d.geo.D + gr] = mi;
+        if constexpr (W32) {
+            // 32-bit counters: this layout's tiles finish on warp 0 at once
+            // (measured faster there than the queue below)
+            if (tid < 32) {
+                if (valid) {
+                    const double N = (double)F;
+                    const double sn = (double)s_snl[tid] / a.fix;
+                    const int o = (int)s_occ[tid];
+                    const double S2 = d.lnN + d.dof.acon[gr] + d.dof.acon[gc] - sn / N + (o - 1.0) / (2.0 * N);
+                    if (d.out.par) d.out.par[par_pair_index(d.out.L, d.geo.nb, d.geo.na, d.geo.nd, gr, gc)] = S2;
+                    if (d.out.mi) {
+                        const double mi = d.dof.s1[gr] + d.dof.s1[gc] - S2;
+                        d.out.mi[(int64_t)gr * d.geo.D + gc] = mi;
+                        d.out.mi[(int64_t)gc * d.geo.D + gr] = mi;
+                    }
                 }
+                // the next tile's epilogue atomics come after its first barrier
+                s_snl[tid] = 0ull;
+                s_occ[tid] = 0u;
+                s_heavy[tid] = 0;
             }
+            continue;
+        }
+        const int q = it & (kQueue - 1);
+        if (tid < 32) {
+            s_qsnl[q][tid] = s_snl[tid];
+            s_qocc[q][tid] = s_occ[tid];
             // the next tile's epilogue atomics come after its first barrier
             s_snl[tid] = 0ull;
             s_occ[tid] = 0u;
             s_heavy[tid] = 0;
+        }
+        if (q == kQueue - 1 || t + gridDim.x >= a.n_tiles) {
+            __syncthreads();
+            // warp w finishes queued tile w: this CTA's tile q - w before t
+            // (the same expression as every other pair kernel and the branch
+            // above, so bodies agree bit for bit); warp 0 refills the queue
+            // only after the next tile's barrier before its epilogue, which
+            // every warp reaches after this
+            if (warp <= q) {
+                const int64_t tq = t - (int64_t)(q - warp) * gridDim.x;
+                const SysDesc &dq = sys_of(tq);
+                const PairTile tl = a.tiles[tq];
+                const int r = pr < tl.nrow ? tl.row0 + pr : -1, c = pc < tl.ncol ? tl.col0 + pc : -1;
+                if (r >= 0 && c >= 0 && r < c) {
+                    const double N = (double)dq.geo.F;
+                    const double sn = (double)s_qsnl[warp][lane] / a.fix;
+                    const int o = (int)s_qocc[warp][lane];
+                    const double S2 = dq.lnN + dq.dof.acon[r] + dq.dof.acon[c] - sn / N + (o - 1.0) / (2.0 * N);
+                    if (dq.out.par) dq.out.par[par_pair_index(dq.out.L, dq.geo.nb, dq.geo.na, dq.geo.nd, r, c)] = S2;
+                    if (dq.out.mi) {
+                        const double mi = dq.dof.s1[r] + dq.dof.s1[c] - S2;
+                        dq.out.mi[(int64_t)r * dq.geo.D + c] = mi;
+                        dq.out.mi[(int64_t)c * dq.geo.D + r] = mi;
+                    }
+                }
+            }
         }
     }
 }
