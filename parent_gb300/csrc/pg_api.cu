@@ -809,7 +809,10 @@ PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_devic
     CK(ctx->bc_out.ensure((size_t)(3 * (int64_t)nd + 3) * ld * es));
     CK(ctx->bc_soa.ensure((size_t)3 * na * lds * sizeof(float)));
     if (!double_prec) CK(ctx->bc_tmp.ensure((size_t)nd * lds * sizeof(double)));
-    if (!xyz_on_device) CK(ctx->bc_stage.ensure((size_t)fc * na * 3 * sizeof(float)));
+    // host coordinates the GPU can read go straight into the transpose (one
+    // read over the host link), the others through a staging copy
+    const bool stage = !xyz_on_device && !host_readable(xyz);
+    if (stage) CK(ctx->bc_stage.ensure((size_t)fc * na * 3 * sizeof(float)));
     CK(ctx->bc_tab.ensure((size_t)nd * (sizeof(int4) + sizeof(int))));
     int4 *d_atoms = (int4 *)ctx->bc_tab.p;
     int *d_parent = (int *)(d_atoms + nd);
@@ -821,7 +824,7 @@ PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_devic
     for (int64_t f0 = 0; f0 < F; f0 += fc) {
         const int n = (int)std::min<int64_t>(fc, F - f0);
         const float *src = xyz + (size_t)f0 * na * 3;
-        if (!xyz_on_device) {
+        if (stage) {
             CK(cudaMemcpyAsync(ctx->bc_stage.p, src, (size_t)n * na * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
             src = (const float *)ctx->bc_stage.p;
         }

@@ -77,23 +77,26 @@ __global__ void __launch_bounds__(512) host_pull_kernel(const uint4 *__restrict_
 // Copies `bytes` from host memory to the device with a pull kernel when the
 // GPU can read `src` directly and both addresses and the size are 16-byte
 // multiples; with a copy-engine copy otherwise. *pulled says which.
+bool host_readable(const void *src) {
+    bool readable = false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, src) == cudaSuccess) {
+        if (at.type == cudaMemoryTypeHost && at.devicePointer == src) readable = true;
+        if (at.type == cudaMemoryTypeUnregistered) {
+            int dev = 0, pma = 0;
+            cudaGetDevice(&dev);
+            readable = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && pma;
+        }
+    }
+    cudaGetLastError();
+    return readable;
+}
+
 cudaError_t h2d_copy(void *dst, const void *src, size_t bytes, cudaStream_t st, bool *pulled) {
     *pulled = false;
     if (bytes == 0) return cudaSuccess;
     const bool aligned = (((uintptr_t)dst | (uintptr_t)src | bytes) & 15) == 0;
-    bool readable = false;
-    if (aligned) {
-        cudaPointerAttributes at;
-        if (cudaPointerGetAttributes(&at, src) == cudaSuccess) {
-            if (at.type == cudaMemoryTypeHost && at.devicePointer == src) readable = true;
-            if (at.type == cudaMemoryTypeUnregistered) {
-                int dev = 0, pma = 0;
-                cudaGetDevice(&dev);
-                readable = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && pma;
-            }
-        }
-        cudaGetLastError();
-    }
+    const bool readable = aligned && host_readable(src);
     if (!readable) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);

@@ -256,6 +256,9 @@ cudaError_t launch_bat_phase(double *dtmp, int64_t ldt, int nf, int nd, const in
 // Host -> device copy by SM loads where the GPU can read the host memory
 // (pg_ingest.cu), else by the copy engine.
 cudaError_t h2d_copy(void *dst, const void *src, size_t bytes, cudaStream_t st, bool *pulled);
+// Host memory this GPU's kernels can read directly: pinned, or pageable where
+// the device has pageable memory access (a Grace-attached part).
+bool host_readable(const void *src);
 
 // A kernel whose bounded mbarrier wait nothing completes (sets err[ERR_TIMEOUT]).
 cudaError_t launch_wait_timeout_probe(long long limit_cycles, int *err, cudaStream_t st);
