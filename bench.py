@@ -105,6 +105,9 @@ def hist_layout(bins: int) -> str:
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--shard", action="store_true",
+                    help="one system split over the ranks (tile shards, one SUM reduction, MIST on rank 0; "
+                         "strong scaling) instead of one independent system per rank")
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
@@ -498,9 +501,128 @@ def run_batch(args):
     return 0
 
 
+def run_sharded(args):
+    """One system split over the ranks (strong scaling), the reference's MPI
+    decomposition GB300 style: every rank preprocesses the whole system and
+    computes its range of the pair tiles (pg_entropy_shard) into a device
+    tensor, one SUM reduction (NCCL) merges the shards on rank 0 without a
+    host copy, and rank 0 runs MIST from the merged device body. A step is
+    that whole sequence; units = the system's updates; time = max over ranks,
+    CUDA events on the framework stream around the steps. e2e: the same with
+    the columns in pinned host memory, uploaded by every rank inside each
+    step, and the merged body and edges read back on rank 0. Rank 0 checks
+    the merged body against a one-GPU pg_entropy body, bit for bit."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import parent_gb300 as pg
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n_atoms, F, prec, fbd, fbb, lat = WORKLOADS[args.workload]
+    n_dih = n_atoms - 3
+    D = 3 * n_atoms - 6
+    units = D * (D - 1) // 2 * F
+    bins = (args.bins,) * 6
+    es = 8 if prec else 4
+    eng = pg.Engine(local)
+    nb, na = n_dih + 2, n_dih + 1
+    dbuf = eng.alloc(D * F * es)
+    ptrs = (dbuf, dbuf + nb * F * es, dbuf + (nb + na) * F * es)
+    eng.synth_device(n_atoms, F, prec, ptrs, F, seed=20260, n_latents=lat, frac_bimodal_dih=fbd,
+                     frac_bimodal_bond=fbb)  # the same system on every rank
+    view = pg.BatView(n_dih, F, prec, 1, F, *ptrs)
+    total = sum(pg.block_sizes(n_dih).values())
+    merged = torch.zeros(total, dtype=torch.float64, device=f"cuda:{local}")
+    torch.cuda.synchronize(local)
+    body = pg.DeviceParBody(n_dih, merged.data_ptr())
+
+    def step(v):
+        eng.entropy_shard(v, bins, rank, world, "hist", out=body)  # returns with the shard written
+        if dist:
+            dist.reduce(merged, dst=0, op=dist.ReduceOp.SUM)
+        if rank == 0:
+            torch.cuda.current_stream().synchronize()
+            return eng.mist(n_dih, body)
+        return None
+
+    for _ in range(args.warmup):
+        step(view)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(local)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    launches0 = eng.launch_count()
+    for _ in range(args.steps):
+        step(view)
+    ev1.record()
+    torch.cuda.synchronize(local)
+    launches = eng.launch_count() - launches0
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, f"cuda:{local}")
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    # e2e: pinned host columns uploaded by every rank inside each step
+    e2e = None
+    if args.e2e_steps > 0:
+        host = pg.C.c_void_p()
+        pg._check(pg.lib().pg_host_alloc_pinned(D * F * es, C.byref(host)))
+        eng.memcpy(host.value, dbuf, D * F * es, 2)
+        eng.synchronize()
+        hview = pg.BatView(n_dih, F, prec, 0, F, host.value, host.value + nb * F * es,
+                           host.value + (nb + na) * F * es)
+        hbody = np.empty(total)
+        step(hview)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            step(hview)
+            if rank == 0:
+                hbody[:] = merged.cpu().numpy()
+        sec = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dist, f"cuda:{local}")
+        e2e = {"value": units / sec, "unit": UNIT, "h2d_bytes_per_step": D * F * es * world,
+               "d2h_bytes_per_step": total * 8 + (D - 1) * (4 * 4 + 8 + 8), "ms_per_step": sec * 1e3}
+        pg._check(pg.lib().pg_host_free_pinned(host))
+    check = None
+    if rank == 0:
+        whole = eng.entropy(view, bins, "hist").flat()
+        check = {"merged_equals_one_gpu_body": bool(np.array_equal(merged.cpu().numpy().view(np.uint64),
+                                                                   whole.view(np.uint64)))}
+        line = {
+            "metric": METRIC, "value": units / (ms / 1e3 / args.steps), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": args.workload, "n_atoms": n_atoms, "dofs": D, "frames": F,
+                       "input": "fp64" if prec else "fp32", "bins": args.bins, "form": "hist",
+                       "parallelism": f"tile shards x{world}, one SUM reduction, MIST on rank 0",
+                       "l2": "inputs (%.1f GB) larger than L2; no flush" % (D * F * es / 1e9)},
+            "e2e": e2e, "check": check, "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    eng.free(dbuf)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_gb300(args):
     if args.workload == BATCH:
         return run_batch(args)
+    if args.shard:
+        return run_sharded(args)
     import torch
     import parent_gb300 as pg
 

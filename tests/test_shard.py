@@ -158,3 +158,23 @@ def test_gpu_shard_rejects_onehot_and_bad_index():
         with pytest.raises(pg.PGError) as ex:
             eng.entropy_shard(t, (50,) * 6, 2, 2)
         assert ex.value.code == pg.PG_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_bench_shard_mode_one_rank():
+    """bench.py --shard (one system split over the ranks, strong scaling) on
+    one GPU: the contract's keys, and the merged device body equals the
+    one-GPU pg_entropy body bit for bit."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    p = subprocess.run([sys.executable, str(root / "bench.py"), "--shard", "--workload", "plain_294dof_20k",
+                        "--steps", "2", "--warmup", "1", "--e2e-steps", "1"], cwd=root, capture_output=True,
+                       text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    d = json.loads([ln for ln in p.stdout.splitlines() if ln.strip()][-1])
+    assert d["scaling"] == "strong" and d["n_gpus"] == 1 and d["value"] > 0
+    assert d["check"]["merged_equals_one_gpu_body"] is True
+    assert d["e2e"]["value"] > 0 and d["gpu_launches"] > 0
