@@ -90,6 +90,12 @@ __device__ inline void store_bin_run(uint8_t *bins, const SysGeom &g, int d, int
     }
 }
 
+// largest 2D bin count of a geometry's DOF types
+inline int bmax2d(const SysGeom &g) {
+    const int a = g.bins[3] > g.bins[4] ? g.bins[3] : g.bins[4];
+    return a > g.bins[5] ? a : g.bins[5];
+}
+
 __host__ __device__ inline int dof_type(int g, int nb, int na) {
     return g < nb ? TB : (g < nb + na ? TA : TD);
 }
@@ -302,6 +308,7 @@ struct OnehotRun {
     size_t off_sys = 0, off_fin = 0, off_tiles = 0, off_snl = 0, acc_bytes = 0;
     int64_t n_tiles = 0;
     bool pair = true;
+    bool low = false;  // every 2D bin count at most 64
     int D = 0;
 };
 cudaError_t onehot_setup(const SysGeom &g, const uint8_t *bins, const DofArrays &dof, PairOut out, cudaStream_t st,

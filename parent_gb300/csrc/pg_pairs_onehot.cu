@@ -152,6 +152,14 @@ __device__ __forceinline__ uint32_t onehot4(uint32_t w, uint32_t t4) {
     const uint32_t a = (w ^ t4) + 0x7F7F7F7Fu;
     return (~a & 0x80808080u) >> 1;
 }
+// The same for bins below 64: every byte of w ^ t4 is below 64, so adding
+// 0x3F sets its bit 6 exactly when it is nonzero (no carry: 63 + 63 < 128),
+// and the complement's bit 6 is 2.0 in E4M3 with no shift. Three integer
+// operations per four frames.
+__device__ __forceinline__ uint32_t onehot4_low(uint32_t w, uint32_t t4) {
+    const uint32_t a = (w ^ t4) + 0x3F3F3F3Fu;
+    return ~a & 0x40404040u;
+}
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
     asm volatile(
@@ -257,7 +265,8 @@ struct Item {
 // barrier (one cluster-scope release per stage instead of one per builder
 // warp, whose memory barriers stalled the builders). The commit of a stage's
 // MMAs arrives on the "empty" barrier of both CTAs.
-template <bool PAIR>
+// LOW: every 2D bin count of the launch is at most 64 (onehot4_low).
+template <bool PAIR, bool LOW>
 __global__ void __launch_bounds__(kThreads, 1)
 onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tiles, int *err) {
     using C = OhCfg<PAIR>;
@@ -495,10 +504,17 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
                 uint4 o = make_uint4(0u, 0u, 0u, 0u);
                 if (it[j].valid) {
                     const uint4 w = *(const uint4 *)(bb + it[j].soff);
-                    o.x = onehot4(w.x, it[j].t4);
-                    o.y = onehot4(w.y, it[j].t4);
-                    o.z = onehot4(w.z, it[j].t4);
-                    o.w = onehot4(w.w, it[j].t4);
+                    if (LOW) {
+                        o.x = onehot4_low(w.x, it[j].t4);
+                        o.y = onehot4_low(w.y, it[j].t4);
+                        o.z = onehot4_low(w.z, it[j].t4);
+                        o.w = onehot4_low(w.w, it[j].t4);
+                    } else {
+                        o.x = onehot4(w.x, it[j].t4);
+                        o.y = onehot4(w.y, it[j].t4);
+                        o.z = onehot4(w.z, it[j].t4);
+                        o.w = onehot4(w.w, it[j].t4);
+                    }
                     if (nvalid < kKB) {  // last block: frames past F are not data
                         const int v = nvalid - it[j].c16;
                         uint32_t m[4];
@@ -798,13 +814,15 @@ static bool use_pairs() {
 
 // The pair kernel over a tile list (each tile names its system) and the
 // finalize kernel over n_fin systems (largest D max_D).
-static cudaError_t launch_tiles(const OhSys *d_sys, const TcTile *d_tiles, int64_t n_tiles, bool pair,
+// low: every 2D bin count of the launch's systems is at most 64.
+static cudaError_t launch_tiles(const OhSys *d_sys, const TcTile *d_tiles, int64_t n_tiles, bool pair, bool low,
                                 const OhFin *d_fin, int n_fin, int max_D, int *err, cudaStream_t st) {
     cudaError_t e;
     if (n_tiles > 0) {
         if (pair) {
             const size_t smem = (size_t)OhCfg<true>::kSmemBytes;
-            if ((e = cudaFuncSetAttribute(onehot_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            auto kern = low ? onehot_kernel<true, true> : onehot_kernel<true, false>;
+            if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
                 return e;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3((unsigned)(2 * n_tiles));
@@ -818,13 +836,12 @@ static cudaError_t launch_tiles(const OhSys *d_sys, const TcTile *d_tiles, int64
             at[0].val.clusterDim.z = 1;
             cfg.attrs = at;
             cfg.numAttrs = 1;
-            if ((e = cudaLaunchKernelEx(&cfg, onehot_kernel<true>, d_sys, d_tiles, err))) return e;
+            if ((e = cudaLaunchKernelEx(&cfg, kern, d_sys, d_tiles, err))) return e;
         } else {
             const size_t smem = (size_t)OhCfg<false>::kSmemBytes;
-            if ((e = cudaFuncSetAttribute(onehot_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem)))
-                return e;
-            onehot_kernel<false><<<(unsigned)n_tiles, kThreads, smem, st>>>(d_sys, d_tiles, err);
+            auto kern = low ? onehot_kernel<false, true> : onehot_kernel<false, false>;
+            if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+            kern<<<(unsigned)n_tiles, kThreads, smem, st>>>(d_sys, d_tiles, err);
         }
     }
     dim3 fg((max_D + 255) / 256, max_D, n_fin);
@@ -871,6 +888,7 @@ cudaError_t onehot_setup(const SysGeom &g, const uint8_t *bins, const DofArrays 
     run->acc_bytes = p.off_sys - p.off_snl;  // the accumulators up to the descriptors
     run->n_tiles = p.n_tiles;
     run->pair = pair;
+    run->low = bmax2d(g) <= 64;
     run->D = g.D;
     return cudaSuccess;
 }
@@ -880,7 +898,7 @@ cudaError_t onehot_run(const OnehotRun &run, int *err, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(base + run.off_snl, 0, run.acc_bytes, st);
     if (e != cudaSuccess) return e;
     return launch_tiles((const OhSys *)(base + run.off_sys), (const TcTile *)(base + run.off_tiles), run.n_tiles,
-                        run.pair, (const OhFin *)(base + run.off_fin), 1, run.D, err, st);
+                        run.pair, run.low, (const OhFin *)(base + run.off_fin), 1, run.D, err, st);
 }
 
 cudaError_t launch_pairs_onehot(const SysGeom &g, const uint8_t *bins, const DofArrays &dof,
@@ -999,9 +1017,11 @@ cudaError_t launch_pairs_onehot_batch(const std::vector<SysGeom> &gs, void *ws, 
     cudaError_t e = cudaMemsetAsync(base + L.acc_begin, 0, L.acc_end - L.acc_begin, st);
     if (e != cudaSuccess) return e;
     *launches = 2;
+    int bmax = 1;
+    for (const SysGeom &g : gs) bmax = std::max(bmax, bmax2d(g));
     return launch_tiles((const OhSys *)(base + L.off_sys), (const TcTile *)(base + L.off_tiles),
-                        (int64_t)L.tiles.size(), pair, (const OhFin *)(base + L.off_fin), (int)gs.size(), L.max_D,
-                        err, st);
+                        (int64_t)L.tiles.size(), pair, bmax <= 64, (const OhFin *)(base + L.off_fin), (int)gs.size(),
+                        L.max_D, err, st);
 }
 
 int64_t pairs_onehot_tiles(const SysGeom &g) { return plan(g, nullptr, use_pairs()).n_tiles; }
