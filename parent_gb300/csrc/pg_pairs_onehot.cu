@@ -500,9 +500,12 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
             unsigned char *st = stages + s * kStageBytes;
 #pragma unroll
             for (int j = 0; j < kItemsPerThread; j++) {
-                if (it[j].dst == 0xffffffffu) continue;
-                uint4 o = make_uint4(0u, 0u, 0u, 0u);
-                if (it[j].valid) {
+                // every thread has an item in all but the last round
+                if (j == kItemsPerThread - 1 && it[j].dst == 0xffffffffu) continue;
+                uint4 o;
+                {
+                    // a row past the tile's end reads chunk 0 (soff 0) and is
+                    // masked to zero: no branch per item
                     const uint4 w = *(const uint4 *)(bb + it[j].soff);
                     if (LOW) {
                         o.x = onehot4_low(w.x, it[j].t4);
@@ -515,6 +518,8 @@ onehot_kernel(const OhSys *__restrict__ systems, const TcTile *__restrict__ tile
                         o.z = onehot4(w.z, it[j].t4);
                         o.w = onehot4(w.w, it[j].t4);
                     }
+                    const uint32_t vm = 0u - (uint32_t)it[j].valid;
+                    o.x &= vm; o.y &= vm; o.z &= vm; o.w &= vm;
                     if (nvalid < kKB) {  // last block: frames past F are not data
                         const int v = nvalid - it[j].c16;
                         uint32_t m[4];
