@@ -122,6 +122,26 @@ PG_API const char *pg_last_global_error(void);
 PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
                       pg_par_body *out);
 
+/* Uploads the columns of a host view ahead of the pg_entropy call that will
+ * read them: the copy engine moves them into a standby device buffer while
+ * the current call's kernels run, and the next pg_entropy (or
+ * pg_entropy_shard) of the same view (every field equal) uses them instead of
+ * uploading; a call with another view drops the prefetch. Returns once the
+ * copies are queued; the host columns must stay unchanged (and, for the
+ * copies to run asynchronously, in pinned memory) until that call. Replaces
+ * nothing in the reference: the master's per-run read of the next .bat
+ * (PARENT.cpp:443-473) is the step it overlaps. */
+PG_API int pg_prefetch(pg_ctx *ctx, const pg_bat_view *traj);
+
+/* pg_entropy of `traj` that, once traj's own columns are on the device,
+ * queues the upload of `next` (a host view, or NULL) on the copy engine, so
+ * it runs while this call's kernels do; the following call on `next`
+ * (pg_entropy or pg_entropy_ahead) takes the uploaded columns. The way to
+ * overlap a loop over trajectories: call i passes trajectory i + 1 as next.
+ * The host columns of `next` must stay unchanged until that call. */
+PG_API int pg_entropy_ahead(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                            pg_par_body *out, const pg_bat_view *next);
+
 /* MIST (get_PAR_MIST.cpp:272-766). If body != NULL the MI values are formed
  * from it exactly as get_mutual (util.cpp:47-81) does; if body == NULL the MI
  * matrix resident from the last pg_entropy on this context is used.

@@ -131,6 +131,9 @@ def lib() -> C.CDLL:
         "pg_write_info_text": (i, [cp, vp]),
         "pg_synth_host": (i, [C.POINTER(SynthSpec), vp, vp, vp, i64, i]),
         "pg_synth_device": (i, [vp, C.POINTER(SynthSpec), vp, vp, vp, i64]),
+        "pg_prefetch": (i, [vp, C.POINTER(BatView)]),
+        "pg_entropy_ahead": (i, [vp, C.POINTER(BatView), C.POINTER(C.c_int), i, C.POINTER(ParBodyC),
+                                 C.POINTER(BatView)]),
         "pg_probe_smem_red_rate": (i, [vp, dp]),
         "pg_device_alloc": (i, [vp, C.c_size_t, C.POINTER(vp)]),
         "pg_device_free": (i, [vp, vp]),
@@ -290,15 +293,25 @@ class Engine:
         return self._ctx
 
     def entropy(self, traj: Trajectory | BatView, bins=(50,) * 6, form: str | int = "auto",
-                out: ParBody | None = None, keep_result: bool = True) -> ParBody | None:
-        """PARENT.x on a trajectory; returns the .par body (or None if keep_result=False)."""
+                out: ParBody | None = None, keep_result: bool = True,
+                next: Trajectory | BatView | None = None) -> ParBody | None:
+        """PARENT.x on a trajectory; returns the .par body (or None if
+        keep_result=False). next: a host trajectory whose upload runs on the
+        copy engine during this call, for the following call on it
+        (pg_entropy_ahead)."""
         v = traj if isinstance(traj, BatView) else traj.view()
         b = (C.c_int * 6)(*bins)
         f = FORMS[form] if isinstance(form, str) else int(form)
         if keep_result and out is None:
             out = ParBody.empty(v.n_dihedrals)
         body = out.c() if keep_result else None
-        _check(lib().pg_entropy(self._ctx, C.byref(v), b, f, C.byref(body) if body else None), self._ctx)
+        if next is None:
+            _check(lib().pg_entropy(self._ctx, C.byref(v), b, f, C.byref(body) if body else None), self._ctx)
+        else:
+            nv = next if isinstance(next, BatView) else next.view()
+            self._prefetched = (next, nv)  # the host columns stay alive until used
+            _check(lib().pg_entropy_ahead(self._ctx, C.byref(v), b, f, C.byref(body) if body else None,
+                                          C.byref(nv)), self._ctx)
         return out if keep_result else None
 
     def bat_from_cartesian(self, xyz: np.ndarray, dih: np.ndarray, double_prec: int = 1) -> BatView:
@@ -362,6 +375,14 @@ class Engine:
             for k, (v, e) in enumerate(zip(views, ebufs)):
                 res.append((_edges_array(e, 3 * v.n_dihedrals + 2), totals[10 * k:10 * k + 10].copy()))
         return outs, res
+
+    def prefetch(self, traj: Trajectory | BatView) -> None:
+        """Queue the upload of a host view's columns for the next entropy()
+        call on the same view (pg_prefetch): the copy engine moves them while
+        the current work runs."""
+        v = traj if isinstance(traj, BatView) else traj.view()
+        self._prefetched = (traj, v)  # the host columns stay alive until used
+        _check(lib().pg_prefetch(self._ctx, C.byref(v)), self._ctx)
 
     def entropy_shard(self, traj: Trajectory | BatView, bins, shard: int, n_shards: int,
                       form: str | int = "auto", out: "ParBody | DeviceParBody | None" = None):

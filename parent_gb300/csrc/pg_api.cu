@@ -119,6 +119,17 @@ struct pg_ctx {
     std::vector<int64_t> graph_key;
     // host trajectories: uploads run on their own stream, one event per DOF group
     cudaStream_t copy = nullptr;
+    // pg_prefetch: the host columns of the next call, uploaded by the copy
+    // engine into a standby buffer while the current call computes; the next
+    // pg_entropy of the same view swaps it in instead of uploading
+    DevBuf cols_pf;
+    pg_bat_view pf_view{};
+    bool pf_pending = false;
+    cudaEvent_t pf_done = nullptr;
+    // pg_entropy_ahead: the view whose upload the running call queues once
+    // its own columns are in place
+    pg_bat_view ahead_view{};
+    bool ahead_set = false;
     static constexpr int kMaxGroups = 64;
     cudaEvent_t gev[kMaxGroups] = {};
     // ... and the pair launches of consecutive groups alternate between two
@@ -207,6 +218,73 @@ static int setup_geometry(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6],
 }
 
 // Shared front half of pg_entropy / pg_pair_counts: validation, upload,
+static bool same_view(const pg_bat_view &a, const pg_bat_view &b) {
+    return a.n_dihedrals == b.n_dihedrals && a.n_frames == b.n_frames && a.double_prec == b.double_prec &&
+           a.on_device == b.on_device && a.ld == b.ld && a.bonds == b.bonds && a.angles == b.angles &&
+           a.dihedrals == b.dihedrals;
+}
+
+// If pg_prefetch uploaded this host view, its standby buffer becomes the
+// column buffer (ctx->cols, columns DOF-major, n_frames apart) once the
+// upload is done on `st`; returns whether it did. A prefetch of another view
+// is dropped (after its upload ends, so the buffer can be reused).
+static cudaError_t take_prefetch(pg_ctx *ctx, const pg_bat_view *tv, cudaStream_t st, bool *taken) {
+    *taken = false;
+    if (!ctx->pf_pending) return cudaSuccess;
+    ctx->pf_pending = false;
+    if (!same_view(ctx->pf_view, *tv)) return cudaEventSynchronize(ctx->pf_done);
+    std::swap(ctx->cols, ctx->cols_pf);
+    *taken = true;
+    return cudaStreamWaitEvent(st, ctx->pf_done, 0);
+}
+
+// Queues the upload of a host view's columns into the standby buffer on the
+// copy stream (copy engine), after the work already on `after` (the stream
+// carrying the current call's own upload), for the next call of that view.
+static int queue_prefetch(pg_ctx *ctx, const pg_bat_view *traj, cudaStream_t after) {
+    if (!traj || traj->on_device) return fail(ctx, PG_ERR_ARG, "prefetch needs a host view");
+    if (traj->n_dihedrals < 0 || traj->n_frames < 1 || traj->ld < traj->n_frames)
+        return fail(ctx, PG_ERR_ARG, "bad view");
+    if (!traj->bonds || !traj->angles || (traj->n_dihedrals > 0 && !traj->dihedrals))
+        return fail(ctx, PG_ERR_ARG, "null column pointer");
+    if (ctx->pf_pending) CK(cudaEventSynchronize(ctx->pf_done));  // one prefetch at a time
+    ctx->pf_pending = false;
+    if (!ctx->pf_done) CK(cudaEventCreateWithFlags(&ctx->pf_done, cudaEventDisableTiming));
+    const int nd = traj->n_dihedrals, nb = nd + 2, na = nd + 1;
+    const size_t es = elem_size(traj->double_prec), F = (size_t)traj->n_frames;
+    const size_t blk[3] = {(size_t)nb * F * es, (size_t)na * F * es, (size_t)nd * F * es};
+    CK(ctx->cols_pf.ensure(blk[0] + blk[1] + blk[2] + 256));
+    // the standby buffer's last reader (an earlier call's kernels) is done,
+    // and the current call's own upload goes first
+    CK(cudaEventRecord(ctx->ev[5], after));
+    CK(cudaStreamWaitEvent(ctx->copy, ctx->ev[5], 0));
+    char *dst = (char *)ctx->cols_pf.p;
+    const void *src[3] = {traj->bonds, traj->angles, traj->dihedrals};
+    const int cnt[3] = {nb, na, nd};
+    for (int t = 0; t < 3; t++) {
+        if (cnt[t] > 0) {
+            // the copy engine, so the upload runs beside the SMs' work
+            if ((size_t)traj->ld == F)
+                CK(cudaMemcpyAsync(dst, src[t], blk[t], cudaMemcpyHostToDevice, ctx->copy));
+            else
+                CK(cudaMemcpy2DAsync(dst, F * es, src[t], (size_t)traj->ld * es, F * es, cnt[t],
+                                     cudaMemcpyHostToDevice, ctx->copy));
+        }
+        dst += blk[t];
+    }
+    CK(cudaEventRecord(ctx->pf_done, ctx->copy));
+    ctx->pf_view = *traj;
+    ctx->pf_pending = true;
+    return PG_OK;
+}
+
+// The pending pg_entropy_ahead upload, queued after `after`'s work.
+static int queue_ahead(pg_ctx *ctx, cudaStream_t after) {
+    if (!ctx->ahead_set) return PG_OK;
+    ctx->ahead_set = false;
+    return queue_prefetch(ctx, &ctx->ahead_view, after);
+}
+
 // preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
 static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int form) {
     int rc0 = setup_geometry(ctx, tv, bins, form);
@@ -227,13 +305,15 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int f
         const size_t es = elem_size(tv->double_prec);
         ld = tv->n_frames;
         const size_t blk[3] = {(size_t)g.nb * ld * es, (size_t)g.na * ld * es, (size_t)g.nd * ld * es};
+        bool pre = false;
+        CK(take_prefetch(ctx, tv, st, &pre));
         CK(ctx->cols.ensure(blk[0] + blk[1] + blk[2] + 256));
         char *dst = (char *)ctx->cols.p;
         const void *src[3] = {tv->bonds, tv->angles, tv->dihedrals};
         const int cnt[3] = {g.nb, g.na, g.nd};
         for (int t = 0; t < 3; t++) {
             cols[t] = dst;
-            if (cnt[t] > 0) {
+            if (cnt[t] > 0 && !pre) {
                 if (tv->ld == tv->n_frames) {
                     bool pulled = false;
                     CK(h2d_copy(dst, src[t], blk[t], st, &pulled));
@@ -248,6 +328,11 @@ static int run_prep(pg_ctx *ctx, const pg_bat_view *tv, const int bins[6], int f
         if (g.nd == 0) cols[2] = cols[1];
     }
     CK(cudaEventRecord(ctx->ev[1], st));
+    {
+        // pg_entropy_ahead: the next call's columns follow on the copy engine
+        const int rca = queue_ahead(ctx, st);
+        if (rca) return rca;
+    }
 
     CK(ctx->bins.ensure(bins_bytes(g)));
     CK(ctx->dofbuf.ensure(dof_bytes(D)));
@@ -476,11 +561,14 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
 
     CK(cudaEventRecord(ctx->ev[0], st));
     CK(cudaStreamWaitEvent(cs, ctx->ev[0], 0));  // earlier kernels reading the columns are done
+    bool pre = false;  // the columns were uploaded ahead by pg_prefetch
+    CK(take_prefetch(ctx, tv, cs, &pre));
+    CK(ctx->cols.ensure((size_t)D * F * es + 256));
     char *cols = (char *)ctx->cols.p;
     const int lo[3] = {0, g.nb, g.nb + g.na}, cnt[3] = {g.nb, g.na, g.nd};
     const void *src[3] = {tv->bonds, tv->angles, tv->dihedrals};
     for (int k = 0; k < K; k++) {
-        for (int t = 0; t < 3; t++) {
+        for (int t = 0; t < 3 && !pre; t++) {
             const int a = std::max(G[k], lo[t]), b = std::min(G[k + 1], lo[t] + cnt[t]);
             if (a >= b) continue;
             const char *from = (const char *)src[t] + (size_t)(a - lo[t]) * tv->ld * es;
@@ -498,6 +586,11 @@ static int run_streamed(pg_ctx *ctx, const pg_bat_view *tv, pg_par_body *out) {
         CK(cudaEventRecord(ctx->gev[k], cs));
     }
     CK(cudaEventRecord(ctx->ev[4], cs));
+    {
+        // pg_entropy_ahead: the next call's columns follow on the copy engine
+        const int rca = queue_ahead(ctx, cs);
+        if (rca) return rca;
+    }
 
     CK(cudaMemsetAsync(ctx->errw.p, 0, ERR_WORDS * sizeof(int), st));
     int rc = ensure_fix_table(ctx, g.F);
@@ -599,7 +692,8 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->cols, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn, &ctx->nfix,
+    if (ctx->pf_pending) cudaEventSynchronize(ctx->pf_done);
+    for (DevBuf *b : {&ctx->cols, &ctx->cols_pf, &ctx->bins, &ctx->dofbuf, &ctx->par, &ctx->mi, &ctx->nlogn, &ctx->nfix,
                       &ctx->tiles, &ctx->errw, &ctx->scratch, &ctx->counts, &ctx->edges, &ctx->mistscr,
                       &ctx->bc_out, &ctx->bc_stage, &ctx->bc_soa, &ctx->bc_tmp, &ctx->bc_tab, &ctx->mie_body,
                       &ctx->mie_slots, &ctx->mie_lens, &ctx->mie_rows, &ctx->mie_text, &ctx->mie_fb})
@@ -610,6 +704,7 @@ PG_API void pg_destroy(pg_ctx *ctx) {
     if (ctx->copy) cudaStreamSynchronize(ctx->copy);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->pf_done) cudaEventDestroy(ctx->pf_done);
     for (auto &e : ctx->gev)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
@@ -852,6 +947,14 @@ PG_API int pg_bat_from_cartesian(pg_ctx *ctx, const float *xyz, int xyz_on_devic
     return PG_OK;
 }
 
+PG_API int pg_prefetch(pg_ctx *ctx, const pg_bat_view *traj) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->err.clear();
+    cudaGetLastError();  // an error left by an earlier failed call of this thread is not this call's
+    CK(cudaSetDevice(ctx->device));
+    return queue_prefetch(ctx, traj, ctx->stream);
+}
+
 PG_API int pg_entropy(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
                       pg_par_body *out) {
     if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
@@ -970,6 +1073,22 @@ PG_API int pg_shard_mask(int n_dihedrals, const int bins[6], int shard, int n_sh
             }
     }
     return PG_OK;
+}
+
+PG_API int pg_entropy_ahead(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form,
+                            pg_par_body *out, const pg_bat_view *next) {
+    if (!ctx) return fail(nullptr, PG_ERR_ARG, "null context");
+    ctx->ahead_set = false;
+    if (next) {
+        if (next->on_device) return fail(ctx, PG_ERR_ARG, "next must be a host view");
+        ctx->ahead_view = *next;
+        ctx->ahead_set = true;
+    }
+    int rc = pg_entropy(ctx, traj, bins, form, out);
+    // a path that uploaded nothing (device columns) queues it now
+    if (rc == PG_OK && ctx->ahead_set) rc = queue_ahead(ctx, ctx->stream);
+    ctx->ahead_set = false;
+    return rc;
 }
 
 PG_API int pg_entropy_shard(pg_ctx *ctx, const pg_bat_view *traj, const int bins[6], int form, int shard,

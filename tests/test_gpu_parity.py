@@ -682,3 +682,27 @@ def test_random_systems_match_oracle(eng, case):
     want = oracle.pair_counts(t.bonds, t.angles, t.dihedrals, bins, pairs)
     for p, x, y in zip(pairs, got, want):
         assert np.array_equal(x, y), (p, bins)
+
+
+def test_entropy_ahead_and_prefetch_give_the_same_bodies(eng):
+    """pg_entropy_ahead queues the next call's upload on the copy engine and
+    pg_prefetch queues one explicitly: the call that takes the uploaded
+    columns, a call on another view (which drops them) and every later call
+    give the bodies of plain pg_entropy calls, bit for bit."""
+    bins = (50,) * 6
+    ta = _synth_case(40, 9000, 0, seed=61, frac_bimodal_dih=0.2)
+    tb = _synth_case(40, 9000, 0, seed=62, frac_bimodal_dih=0.2)
+    tc = _synth_case(33, 7001, 1, seed=63)
+    want = {k: eng.entropy(t, bins, "hist").flat() for k, t in (("a", ta), ("b", tb), ("c", tc))}
+    same = lambda body, k: np.array_equal(body.flat().view(np.uint64), want[k].view(np.uint64))
+    assert same(eng.entropy(ta, bins, "hist", next=tb), "a")
+    assert same(eng.entropy(tb, bins, "hist", next=tb), "b")   # takes tb's columns, queues tb again
+    assert same(eng.entropy(tb, bins, "hist"), "b")            # takes them again
+    assert same(eng.entropy(ta, bins, "hist", next=tb), "a")
+    assert same(eng.entropy(tc, bins, "hist"), "c")            # another view: the prefetch of tb is dropped
+    assert same(eng.entropy(tb, bins, "hist"), "b")
+    eng.prefetch(tc)
+    assert same(eng.entropy(tc, bins, "hist"), "c")
+    eng.prefetch(ta)
+    part = [eng.entropy_shard(ta, bins, s, 2) for s in range(2)]   # shard 0 takes the prefetched columns
+    assert np.array_equal((part[0].flat() + part[1].flat()).view(np.uint64), want["a"].view(np.uint64))
