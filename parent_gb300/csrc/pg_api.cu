@@ -278,11 +278,18 @@ static int queue_prefetch(pg_ctx *ctx, const pg_bat_view *traj, cudaStream_t aft
     return PG_OK;
 }
 
-// The pending pg_entropy_ahead upload, queued after `after`'s work.
+// The pending pg_entropy_ahead upload, queued after `after`'s work. It only
+// saves time, so a failure to queue it (no memory for the standby buffer,
+// say) drops it and leaves the current call alone: the next call uploads.
 static int queue_ahead(pg_ctx *ctx, cudaStream_t after) {
     if (!ctx->ahead_set) return PG_OK;
     ctx->ahead_set = false;
-    return queue_prefetch(ctx, &ctx->ahead_view, after);
+    if (queue_prefetch(ctx, &ctx->ahead_view, after) != PG_OK) {
+        ctx->pf_pending = false;
+        ctx->err.clear();
+        cudaGetLastError();
+    }
+    return PG_OK;
 }
 
 // preprocessing. Leaves bins, dof arrays and the nlogn table on the device.
