@@ -200,3 +200,13 @@ def test_mie_text_many_rows_matches_python_formatting(tmp_path):
     tot = oracle.mie_totals(n, blocks)
     got_tot = np.array([float(ln.split(" = ")[1]) for ln in lines[len(want):]])
     assert np.array_equal(np.array([float(oracle.fmt12(x)) for x in tot]), got_tot)
+
+
+def test_prefetch_entry_points_reject_a_null_context():
+    """pg_prefetch and pg_entropy_ahead check their context before any CUDA
+    call (CPU: no device needed)."""
+    import ctypes as C
+    v = pg.BatView()
+    b = (C.c_int * 6)(*(50,) * 6)
+    assert pg.lib().pg_prefetch(None, C.byref(v)) == pg.PG_ERR_ARG
+    assert pg.lib().pg_entropy_ahead(None, C.byref(v), b, 0, None, C.byref(v)) == pg.PG_ERR_ARG
